@@ -1,0 +1,164 @@
+/*
+ * marie_gb300.h -- C ABI of the GB300 FFT-VIE operator and GMRES solver.
+ *
+ * Drop-in boundary for MARIE's pure-VIE hot path.  In the reference the path
+ * is reached through the MATLAB function-handle table built by
+ * src/src_utils/src_loaders/parse_inputs.m:6-37 (func.mvp_N, func.mvp_K,
+ * func.mvp_herm_adj_N/K, func.mvp_G, func.mvp_invG) and through
+ *   [x,iter,resvec] = is_gmres_vie(A,b,restart,tol,maxit,x0)
+ * (src/src_solver/src_iterative_solvers/is_gmres_vie.m:1).  A MEX gateway or
+ * any FFI binds the functions below; no C++ or torch type crosses the ABI.
+ *
+ * Conventions
+ *  - Complex numbers are interleaved (re, im) pairs: double for MARIE_C128,
+ *    float for MARIE_C64 (MATLAB R2018a mxComplexDouble / mxComplexSingle).
+ *  - Grids are column-major (n1, n2, n3, C) per right-hand side; body vectors
+ *    have length N_b = C * N_s in component-major blocks, exactly the order
+ *    of idx_solution (src/src_geometry/body_geometry/geo_body_domain.m:22-34).
+ *  - Several right-hand sides are contiguous: rhs r starts at r * len.
+ *  - All vector pointers passed to apply/solve calls are DEVICE pointers
+ *    unless a comment says otherwise; descriptor arrays are HOST pointers.
+ *  - Work is enqueued on the caller's stream (cudaStream_t passed as void*;
+ *    NULL = legacy default stream).  A handle is not thread-safe; distinct
+ *    handles are independent.  No call throws; every call returns a status.
+ */
+#ifndef MARIE_GB300_H
+#define MARIE_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MARIE_OK = 0,
+  MARIE_ERR_BAD_ARG = 1,        /* invalid argument (message via marie_last_error) */
+  MARIE_ERR_OOM = 2,            /* device allocation failed or cap exceeded */
+  MARIE_ERR_NONFINITE = 3,      /* NaN/Inf in an input or an iterate */
+  MARIE_ERR_NOT_CONVERGED = 4,  /* maxit reached; report holds the residual */
+  MARIE_ERR_DEVICE_TIMEOUT = 5, /* a bounded device wait expired */
+  MARIE_ERR_CUDA = 6,           /* CUDA runtime error (code via marie_last_error) */
+  MARIE_ERR_NOT_SUPPORTED = 7   /* valid but unsupported configuration */
+} marie_status;
+
+typedef enum { MARIE_C128 = 0, MARIE_C64 = 1 } marie_precision;
+typedef enum { MARIE_PWC = 0, MARIE_PWL = 1 } marie_basis;
+
+typedef struct marie_vie marie_vie; /* opaque handle */
+
+/* One Tucker block as produced by assembly_fft_circ_tucker_{pwc,pwl}.m:
+ * G is r1 x r2 x r3 (column-major); U1 is r1 x 2*n1, U2 r2 x 2*n2, U3 r3 x 2*n3
+ * (already circulant-extended, FFT'd and transposed). Host pointers. */
+typedef struct {
+  int32_t r1, r2, r3;
+  const double* G;   /* interleaved complex, r1*r2*r3 */
+  const double* U1;  /* interleaved complex, r1*2*n1 */
+  const double* U2;
+  const double* U3;
+} marie_tucker_block;
+
+typedef struct {
+  int32_t n1, n2, n3;        /* grid edges */
+  int32_t basis;             /* MARIE_PWC (C=3) or MARIE_PWL (C=12) */
+  double res;                /* voxel edge [m] */
+  double freq;               /* frequency [Hz] (ce = i*2*pi*freq*eps0) */
+  int64_t n_b;               /* length of idx_solution (= C * N_s) */
+  const int64_t* idx_solution; /* host, 0-based, component-major blocks */
+  const double* Mr;          /* host, n1*n2*n3 interleaved complex (em_assembly.m:14) */
+  /* N operator: either Tucker blocks (count 6 PWC / 60 PWL, index j*6+k for
+   * T(j+1,k+1)) or a dense I_V (n1,n2,n3,pwx,6) column-major; one must be set. */
+  const marie_tucker_block* tucker_N;
+  const double* dense_N;
+  /* K operator (optional): Tucker (3 PWC / 30 PWL, index j*3+k) or dense (n1,n2,n3,pwx,3). */
+  const marie_tucker_block* tucker_K;
+  const double* dense_K;
+  int32_t precisions;        /* bit mask: 1 = build C128 path, 2 = build C64 path */
+  int32_t max_rhs;           /* largest nrhs per apply/solve call (workspace sizing) */
+  int64_t mem_cap_bytes;     /* 0 = no cap; otherwise create/solve fail with OOM above it */
+} marie_vie_desc;
+
+/* Build an operator handle: uploads the body map, contrast and Green's-tensor
+ * spectra and sizes the workspaces.  Replaces the operator set-up of
+ * ie_solver_vie.m:14 (fN = to_GPU(MREDM.operators.N,1)) together with the
+ * per-product Tucker re-expansion of mvp_N_pwl_tucker.m:31 (done once here). */
+marie_status marie_vie_create(marie_vie** h, const marie_vie_desc* d);
+marie_status marie_vie_destroy(marie_vie* h);
+
+/* y = mvp_vie(x): src/src_solver/src_mvp/mvp_vie/mvp_vie.m:1-19
+ * (x, y: nrhs x N_b, precision prec). */
+marie_status marie_vie_apply(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
+/* y = A^H x for A = mvp_vie: y = x - N^H(invG .* conj(Mc./Mr) .* x), with N^H
+ * from mvp_N_herm_adj_{pwc,pwl}_tucker.m. */
+marie_status marie_vie_apply_adjoint(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
+/* Raw operators on full grids (nrhs x n1*n2*n3*C):
+ * mvp_N_{pwc,pwl}_tucker.m:1-33/43, mvp_N_herm_adj_{pwc,pwl}_tucker.m,
+ * mvp_K_{pwc,pwl}_tucker.m:1-36/45, mvp_K_herm_adj_{pwc,pwl}_tucker.m. */
+marie_status marie_vie_apply_N(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
+marie_status marie_vie_apply_N_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
+marie_status marie_vie_apply_K(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
+marie_status marie_vie_apply_K_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
+
+typedef enum {
+  MARIE_SOLVE_FP64 = 0,   /* complex128 GMRES, faithful to is_gmres_vie.m */
+  MARIE_SOLVE_MIXED = 1   /* complex64 GMRES inside an FP64 iterative-refinement loop */
+} marie_solve_mode;
+
+typedef struct {
+  int32_t restart;        /* is_gmres_vie restart (reference: 50) */
+  int32_t maxit;          /* max restart cycles (reference: 200) */
+  double tol;             /* relative residual target */
+  int32_t mode;           /* marie_solve_mode */
+  int32_t x0_present;     /* 1: x holds the initial guess; 0: start from zero */
+  double inner_tol;       /* MIXED: inner c64 GMRES relative tolerance (e.g. 1e-4) */
+  int32_t max_refine;     /* MIXED: max refinement steps */
+} marie_gmres_opts;
+
+typedef struct {
+  int32_t* iters;         /* host, per rhs: total inner iterations (may be NULL) */
+  int32_t* outer;         /* host, per rhs: restart cycles (iter(2) of is_gmres_vie) */
+  int32_t* last_inner;    /* host, per rhs: iterations in the last cycle (iter(1)) */
+  double* true_resid;     /* host, per rhs: ||b - A x|| / ||b|| recomputed in FP64 */
+  double* resvec;         /* host, per rhs x resvec_cap: relative residual history (may be NULL) */
+  int32_t resvec_cap;
+  int32_t* resvec_len;    /* host, per rhs */
+  int32_t* status;        /* host, per rhs: marie_status */
+  int32_t matvecs_c128;   /* out: FP64 operator applications per rhs batch */
+  int32_t matvecs_c64;    /* out: complex64 operator applications */
+} marie_gmres_report;
+
+/* [x,iter,resvec] = is_gmres_vie(A,b,restart,tol,maxit,x0) with A = mvp_vie,
+ * for nrhs independent right-hand sides in one batched launch sequence
+ * (src/src_solver/src_iterative_solvers/is_gmres_vie.m:1-30,
+ *  is_iter_gmres_vie.m:1-38; the serial port loop of ie_solver_vie.m:16-21).
+ * b and x are device complex128 (nrhs x N_b). */
+marie_status marie_gmres_vie(marie_vie* h, const void* b, void* x, int32_t nrhs,
+                             const marie_gmres_opts* opts, marie_gmres_report* report, void* stream);
+
+/* Operator-generation helpers (producers of the hot path's operands). */
+/* I_V of assembly_N.m / assembly_K.m (far and medium zones by 6D Gauss rules,
+ * near zone {0,1}^3 by the staggered stand-in rule); out: host, dense
+ * (n1,n2,n3,pwx,6|3) interleaved complex.  kernel: 0 = N, 1 = K. */
+marie_status marie_assemble_green(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
+                                  int32_t basis, int32_t kernel, double* out_host);
+/* Incident field of closed loops with unit current, tested onto the PWC/PWL
+ * basis (coef_l = int E.f_l / int f_l^2): the loop/wire RHS generator.
+ * loops: host, nloop x 6 doubles (centre xyz, normal xyz); out: device
+ * complex128, nloop x N_b.  voxel centres: centre of voxel (0,0,0) = origin. */
+marie_status marie_incident_loops(marie_vie* h, const double* origin, const double* loops, int32_t nloop,
+                                  double radius, int32_t nseg, void* out_dev, void* stream);
+/* Unit x-polarised plane wave exp(-i k0 z) tested onto the basis. */
+marie_status marie_incident_plane_wave(marie_vie* h, const double* origin, void* out_dev, void* stream);
+
+/* Diagnostics. */
+const char* marie_last_error(void);
+const char* marie_version(void);
+/* Number of kernel launches issued by this library since load. */
+int64_t marie_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MARIE_GB300_H */

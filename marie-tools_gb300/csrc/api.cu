@@ -1,0 +1,500 @@
+// C-ABI entry points of the operator: create/destroy/apply, plus the FFT
+// plans, per-axis tables and the matvec launcher.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <complex>
+#include <mutex>
+#include <new>
+
+#include "internal.h"
+
+namespace marie {
+
+static thread_local std::string t_err;
+std::atomic<int64_t> g_launches{0};
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_err = buf;
+}
+
+marie_status dev_alloc(marie_vie* h, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) return MARIE_OK;
+  if (h->mem_cap > 0 && h->mem_used + (int64_t)bytes > h->mem_cap) {
+    set_error("device memory cap exceeded: need %lld more bytes, cap %lld, used %lld",
+              (long long)bytes, (long long)h->mem_cap, (long long)h->mem_used);
+    return MARIE_ERR_OOM;
+  }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    *p = nullptr;
+    return MARIE_ERR_OOM;
+  }
+  h->allocs.push_back(*p);
+  h->mem_used += (int64_t)bytes;
+  return MARIE_OK;
+}
+
+void dev_free_all(marie_vie* h) {
+  for (void* p : h->allocs) cudaFree(p);
+  h->allocs.clear();
+  h->mem_used = 0;
+}
+
+template <>
+PrecState<double>& prec_state<double>(marie_vie* h) { return h->p64; }
+template <>
+PrecState<float>& prec_state<float>(marie_vie* h) { return h->p32; }
+
+// n = product of radices; 8s first, then 4, 2, then odd primes.
+static bool make_plan(int n, FftPlan* pl) {
+  pl->n = n;
+  pl->nst = 0;
+  int m = n;
+  auto push = [&](int r) {
+    if (pl->nst >= kMaxStages) return false;
+    pl->r[pl->nst++] = r;
+    m /= r;
+    return true;
+  };
+  while (m % 8 == 0) if (!push(8)) return false;
+  if (m % 4 == 0) if (!push(4)) return false;
+  if (m % 2 == 0) if (!push(2)) return false;
+  for (int p = 3; m > 1 && p <= 31; p += 2) {
+    while (m % p == 0) if (!push(p)) return false;
+  }
+  return m == 1;
+}
+
+// kofp[p]: frequency held at digit-reversed position p (see FftPlan).
+static void digit_maps(const FftPlan& pl, std::vector<int>& kofp, std::vector<int>& pofk) {
+  const int n = pl.n;
+  kofp.assign(n, 0);
+  pofk.assign(n, 0);
+  for (int k = 0; k < n; ++k) {
+    int rem = k, p = 0, span = n;
+    for (int s = 0; s < pl.nst; ++s) {
+      const int r = pl.r[s];
+      const int t = rem % r;
+      rem /= r;
+      span /= r;
+      p += t * span;
+    }
+    kofp[p] = k;
+    pofk[k] = p;
+  }
+}
+
+template <typename T>
+static marie_status build_axis(marie_vie* h, int n, AxisDev<T>& ax) {
+  if (!make_plan(n, &ax.plan)) {
+    set_error("grid edge %d has a prime factor above 31 (unsupported FFT length)", n);
+    return MARIE_ERR_NOT_SUPPORTED;
+  }
+  std::vector<cplx<T>> tw(n), tw2(n);
+  for (int k = 0; k < n; ++k) {
+    const long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)n;
+    const long double b = a / 2.0L;
+    tw[k] = cplx<T>{(T)std::cos(a), (T)std::sin(a)};
+    tw2[k] = cplx<T>{(T)std::cos(b), (T)std::sin(b)};
+  }
+  std::vector<int> kofp, pofk;
+  digit_maps(ax.plan, kofp, pofk);
+  MARIE_TRY(dev_alloc(h, (void**)&ax.tw, n * sizeof(cplx<T>)));
+  MARIE_TRY(dev_alloc(h, (void**)&ax.tw2, n * sizeof(cplx<T>)));
+  MARIE_TRY(dev_alloc(h, (void**)&ax.kofp, n * sizeof(int)));
+  MARIE_TRY(dev_alloc(h, (void**)&ax.pofk, n * sizeof(int)));
+  MARIE_CUDA_TRY(cudaMemcpy(ax.tw, tw.data(), n * sizeof(cplx<T>), cudaMemcpyHostToDevice));
+  MARIE_CUDA_TRY(cudaMemcpy(ax.tw2, tw2.data(), n * sizeof(cplx<T>), cudaMemcpyHostToDevice));
+  MARIE_CUDA_TRY(cudaMemcpy(ax.kofp, kofp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  MARIE_CUDA_TRY(cudaMemcpy(ax.pofk, pofk.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  return MARIE_OK;
+}
+
+// Block tables of mvp_{N,K}{,_herm_adj}_{pwc,pwl}_tucker.m.
+static const int PQ_N[3][3] = {{1, 2, 3}, {2, 4, 5}, {3, 5, 6}};
+static const int PQ_K[3][3] = {{0, -3, 2}, {3, 0, -1}, {-2, 1, 0}};
+static const int LLP[4][4] = {{1, 5, 6, 7}, {-5, 2, 8, 9}, {-6, 8, 3, 10}, {-7, 9, 10, 4}};
+static const int SLP[4][4] = {{1, -1, -1, -1}, {-1, 1, 1, 1}, {-1, 1, 1, 1}, {-1, 1, 1, 1}};
+// circulant mirror signs, assembly_fft_circ_tucker_{pwc,pwl}.m
+static const int GN1[6] = {+1, -1, -1, +1, +1, +1}, GN2[6] = {+1, -1, +1, +1, -1, +1},
+                 GN3[6] = {+1, +1, -1, +1, -1, +1};
+static const int GK1[3] = {-1, +1, +1}, GK2[3] = {+1, -1, +1}, GK3[3] = {+1, +1, -1};
+static const int BT1[10] = {+1, +1, +1, +1, -1, +1, +1, -1, -1, +1};
+static const int BT2[10] = {+1, +1, +1, +1, +1, -1, +1, -1, +1, -1};
+static const int BT3[10] = {+1, +1, +1, +1, +1, +1, -1, +1, -1, -1};
+
+static inline int sgn(int v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
+
+static void make_tables(marie_vie* h) {
+  const int C = h->C, pwl = h->pwl;
+  for (int t = 0; t < 4; ++t) {
+    BlockTab& b = h->tab[t];
+    memset(&b, 0, sizeof(b));
+    for (int i = 0; i < kMaxComp * kMaxComp; ++i) b.blk[i] = -1;
+    const bool isK = t >= 2, adj = (t & 1) != 0;
+    const int ncomp = isK ? 3 : 6;
+    const int pwx = pwl ? 10 : 1;
+    b.nblk = pwx * ncomp;
+    b.conj = adj ? 1 : 0;
+    for (int j = 0; j < pwx; ++j)
+      for (int k = 0; k < ncomp; ++k) {
+        const int id = j * ncomp + k;
+        const int bt1 = pwl ? BT1[j] : 1, bt2 = pwl ? BT2[j] : 1, bt3 = pwl ? BT3[j] : 1;
+        b.s1[id] = (int8_t)((isK ? GK1[k] : GN1[k]) * bt1);
+        b.s2[id] = (int8_t)((isK ? GK2[k] : GN2[k]) * bt2);
+        b.s3[id] = (int8_t)((isK ? GK3[k] : GN3[k]) * bt3);
+      }
+    for (int p = 0; p < 3; ++p)
+      for (int q = 0; q < 3; ++q) {
+        int k, s_pq;
+        if (!isK) {
+          k = PQ_N[p][q] - 1;
+          s_pq = 1;
+        } else {
+          if (p == q) continue;
+          k = std::abs(PQ_K[p][q]) - 1;
+          s_pq = sgn(PQ_K[p][q]);
+        }
+        if (!pwl) {
+          int s = s_pq;
+          if (isK && adj) s = -s;  // conj(-nmp(...)), mvp_K_herm_adj_pwc_tucker.m:26
+          b.blk[p * C + q] = (int8_t)k;
+          b.sgn[p * C + q] = (int8_t)s;
+          continue;
+        }
+        for (int l = 0; l < 4; ++l)
+          for (int lp = 0; lp < 4; ++lp) {
+            const int j = std::abs(LLP[l][lp]) - 1;
+            int s = s_pq * sgn(LLP[l][lp]);
+            if (adj) {
+              s *= sgn(SLP[l][lp]);
+              if (isK) s = -s;  // mvp_K_herm_adj_pwl_tucker.m:34
+            }
+            const int row = 4 * p + l, col = 4 * q + lp;
+            b.blk[row * C + col] = (int8_t)(j * ncomp + k);
+            b.sgn[row * C + col] = (int8_t)s;
+          }
+      }
+  }
+}
+
+template <typename T>
+static void choose_tiles(marie_vie* h, PrecState<T>& ps) {
+  const int n1 = h->n1, n2 = h->n2, n3 = h->n3, C = h->C;
+  const int sz = (int)sizeof(cplx<T>);
+  ps.TY = std::max(1, std::min(n2, (sizeof(T) == 4 ? 2048 : 1024) / std::max(1, n1)));
+  ps.TXY = std::max(1, std::min(2 * n1, sizeof(T) == 4 ? 16 : 8));
+  int TX = 32;
+  while (TX > 1 && (size_t)n3 * (2 * C * TX + 1) * sz > 100 * 1024) TX /= 2;
+  ps.TX = std::max(1, std::min(TX, 2 * n1));
+}
+
+template <typename T>
+static void fill_axis(AxisTab<T>& dst, const AxisDev<T>& src) {
+  dst.tw = src.tw;
+  dst.tw2 = src.tw2;
+  dst.kofp = src.kofp;
+  dst.pofk = src.pofk;
+  dst.plan = src.plan;
+}
+
+static int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  if (!v || !*v) return dflt;
+  return atoi(v);
+}
+
+template <typename T>
+static marie_status alloc_workspace(marie_vie* h, PrecState<T>& ps) {
+  const int64_t per = (int64_t)h->C * h->n3 * h->n2 * 2 * h->n1;  // T1 per rhs
+  int ws = std::max(1, std::min(h->max_rhs, env_int("MARIE_WS_RHS", 16)));
+  ps.ws_rhs = ws;
+  MARIE_TRY(dev_alloc(h, (void**)&ps.T1, (size_t)ws * per * sizeof(cplx<T>)));
+  MARIE_TRY(dev_alloc(h, (void**)&ps.S, (size_t)ws * per * 2 * sizeof(cplx<T>)));
+  return MARIE_OK;
+}
+
+template <typename T>
+static void set_smem_attr(const void* fn) {
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+template <typename T>
+marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
+                           int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream) {
+  PrecState<T>& ps = prec_state<T>(h);
+  if (!ps.built) {
+    set_error("precision not built for this handle");
+    return MARIE_ERR_BAD_ARG;
+  }
+  const bool isK = op == OP_K || op == OP_K_ADJ;
+  if (isK && !h->has_K) {
+    set_error("K operator was not supplied at create time");
+    return MARIE_ERR_BAD_ARG;
+  }
+  static std::once_flag once;
+  std::call_once(once, [] {
+    set_smem_attr<T>((const void*)k_fwd_x<float>);
+    set_smem_attr<T>((const void*)k_fwd_y<float>);
+    set_smem_attr<T>((const void*)k_z<float, 3>);
+    set_smem_attr<T>((const void*)k_z<float, 12>);
+    set_smem_attr<T>((const void*)k_inv_y<float>);
+    set_smem_attr<T>((const void*)k_inv_x<float>);
+    set_smem_attr<T>((const void*)k_fwd_x<double>);
+    set_smem_attr<T>((const void*)k_fwd_y<double>);
+    set_smem_attr<T>((const void*)k_z<double, 3>);
+    set_smem_attr<T>((const void*)k_z<double, 12>);
+    set_smem_attr<T>((const void*)k_inv_y<double>);
+    set_smem_attr<T>((const void*)k_inv_x<double>);
+  });
+  MvArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.n1 = h->n1;
+  a.n2 = h->n2;
+  a.n3 = h->n3;
+  a.C = h->C;
+  a.Ns = h->Ns;
+  a.mode = mode;
+  fill_axis(a.ax, ps.ax);
+  fill_axis(a.ay, ps.ay);
+  fill_axis(a.az, ps.az);
+  a.vox2sol = h->vox2sol;
+  a.chi = ps.chi;
+  for (int c = 0; c < h->C; ++c) a.invg[c] = (T)h->invg[c];
+  a.T1 = ps.T1;
+  a.S = ps.S;
+  a.G = isK ? ps.GK : ps.GN;
+  a.TY = ps.TY;
+  a.TXY = ps.TXY;
+  a.TX = ps.TX;
+  a.in_rs = in_rs;
+  a.out_rs = out_rs;
+  const BlockTab& bt = h->tab[op];
+  const int n1 = h->n1, n2 = h->n2, n3 = h->n3, C = h->C;
+  const size_t sz = sizeof(cplx<T>);
+  const size_t smx = (size_t)(n1 + 2 * a.TY * n1) * sz;
+  const size_t smy = (size_t)(n2 + 2 * n2 * a.TXY) * sz;
+  const size_t smz = (size_t)(n3 + (size_t)n3 * (2 * C * a.TX + 1)) * sz;
+  for (int r0 = 0; r0 < nrhs; r0 += ps.ws_rhs) {
+    const int nr = std::min(ps.ws_rhs, nrhs - r0);
+    a.nrhs = nr;
+    a.in = in + (int64_t)r0 * in_rs;
+    a.out = out + (int64_t)r0 * out_rs;
+    a.active = active ? active + r0 : nullptr;
+    dim3 gx((n2 + a.TY - 1) / a.TY, n3, nr * C);
+    dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nr * C);
+    dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nr);
+    k_fwd_x<T><<<gx, 256, smx, stream>>>(a);
+    MARIE_LAUNCH_CHECK();
+    k_fwd_y<T><<<gy, 256, smy, stream>>>(a);
+    MARIE_LAUNCH_CHECK();
+    if (C == 12) k_z<T, 12><<<gz, 256, smz, stream>>>(a, bt);
+    else k_z<T, 3><<<gz, 256, smz, stream>>>(a, bt);
+    MARIE_LAUNCH_CHECK();
+    k_inv_y<T><<<gy, 256, smy, stream>>>(a);
+    MARIE_LAUNCH_CHECK();
+    k_inv_x<T><<<gx, 256, smx, stream>>>(a);
+    MARIE_LAUNCH_CHECK();
+  }
+  return MARIE_OK;
+}
+
+template marie_status launch_matvec<float>(marie_vie*, int, int, const cplx<float>*, int64_t, cplx<float>*, int64_t,
+                                           int, const unsigned char*, cudaStream_t);
+template marie_status launch_matvec<double>(marie_vie*, int, int, const cplx<double>*, int64_t, cplx<double>*,
+                                            int64_t, int, const unsigned char*, cudaStream_t);
+
+}  // namespace marie
+
+using namespace marie;
+
+static marie_status validate_desc(const marie_vie_desc* d, std::vector<int64_t>& idxS) {
+  if (!d) { set_error("desc is NULL"); return MARIE_ERR_BAD_ARG; }
+  if (d->n1 < 1 || d->n2 < 1 || d->n3 < 1 || d->n1 > kMaxAxis || d->n2 > kMaxAxis || d->n3 > kMaxAxis) {
+    set_error("grid edges must be in [1, %d], got %d x %d x %d", kMaxAxis, d->n1, d->n2, d->n3);
+    return MARIE_ERR_BAD_ARG;
+  }
+  if (d->basis != MARIE_PWC && d->basis != MARIE_PWL) { set_error("basis must be 0 (PWC) or 1 (PWL)"); return MARIE_ERR_BAD_ARG; }
+  if (!(d->res > 0) || !std::isfinite(d->res)) { set_error("res must be a positive finite number"); return MARIE_ERR_BAD_ARG; }
+  if (!(d->freq > 0) || !std::isfinite(d->freq)) { set_error("freq must be a positive finite number"); return MARIE_ERR_BAD_ARG; }
+  if (!d->idx_solution || d->n_b <= 0) { set_error("idx_solution is empty"); return MARIE_ERR_BAD_ARG; }
+  if (!d->Mr) { set_error("Mr is NULL"); return MARIE_ERR_BAD_ARG; }
+  if (!d->tucker_N && !d->dense_N) { set_error("neither tucker_N nor dense_N given"); return MARIE_ERR_BAD_ARG; }
+  if (d->precisions < 1 || d->precisions > 3) { set_error("precisions must be 1, 2 or 3"); return MARIE_ERR_BAD_ARG; }
+  if (d->max_rhs < 1) { set_error("max_rhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
+  const int C = d->basis == MARIE_PWL ? 12 : 3;
+  if (d->n_b % C != 0) { set_error("n_b=%lld is not a multiple of %d components", (long long)d->n_b, C); return MARIE_ERR_BAD_ARG; }
+  const int64_t Ns = d->n_b / C;
+  const int64_t nD = (int64_t)d->n1 * d->n2 * d->n3;
+  if (Ns > nD) { set_error("more body voxels than grid voxels"); return MARIE_ERR_BAD_ARG; }
+  idxS.assign(d->idx_solution, d->idx_solution + Ns);
+  for (int64_t s = 0; s < Ns; ++s)
+    if (idxS[s] < 0 || idxS[s] >= nD) {
+      set_error("idx_solution[%lld]=%lld outside the grid", (long long)s, (long long)idxS[s]);
+      return MARIE_ERR_BAD_ARG;
+    }
+  for (int c = 1; c < C; ++c)
+    for (int64_t s = 0; s < Ns; ++s)
+      if (d->idx_solution[c * Ns + s] != c * nD + idxS[s]) {
+        set_error("idx_solution is not component-major (block %d, entry %lld)", c, (long long)s);
+        return MARIE_ERR_BAD_ARG;
+      }
+  return MARIE_OK;
+}
+
+extern "C" {
+
+marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
+  if (!out) { set_error("output handle pointer is NULL"); return MARIE_ERR_BAD_ARG; }
+  *out = nullptr;
+  std::vector<int64_t> idxS;
+  MARIE_TRY(validate_desc(d, idxS));
+  marie_vie* h = new (std::nothrow) marie_vie();
+  if (!h) { set_error("host allocation failed"); return MARIE_ERR_OOM; }
+  h->n1 = d->n1; h->n2 = d->n2; h->n3 = d->n3;
+  h->pwl = d->basis == MARIE_PWL;
+  h->C = h->pwl ? 12 : 3;
+  h->res = d->res;
+  h->freq = d->freq;
+  const double mu0 = 4e-7 * M_PI, c0 = 299792458.0;
+  const double e0 = 1.0 / (c0 * c0 * mu0);
+  h->omega = 2 * M_PI * d->freq;
+  h->k0 = 2 * M_PI / (c0 / d->freq);
+  h->Nb = d->n_b;
+  h->Ns = d->n_b / h->C;
+  h->max_rhs = d->max_rhs;
+  h->precisions = d->precisions;
+  h->mem_cap = d->mem_cap_bytes;
+  h->has_K = (d->tucker_K || d->dense_K) ? 1 : 0;
+  h->nblkN = (h->pwl ? 10 : 1) * 6;
+  h->nblkK = (h->pwl ? 10 : 1) * 3;
+  h->idxS_host = idxS;
+  const double r3 = d->res * d->res * d->res;
+  for (int c = 0; c < h->C; ++c) h->invg[c] = (h->pwl && (c % 4) != 0) ? 1.0 / (r3 / 12.0) : 1.0 / r3;
+  make_tables(h);
+  auto fail = [&](marie_status s) {
+    dev_free_all(h);
+    delete h;
+    return s;
+  };
+  if (cudaGetDevice(&h->device) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("no CUDA device available");
+    return fail(MARIE_ERR_CUDA);
+  }
+  // body map
+  const int64_t nD = (int64_t)h->n1 * h->n2 * h->n3;
+  std::vector<int> vox(nD, -1);
+  for (int64_t s = 0; s < h->Ns; ++s) {
+    if (vox[idxS[s]] != -1) { set_error("idx_solution lists voxel %lld twice", (long long)idxS[s]); return fail(MARIE_ERR_BAD_ARG); }
+    vox[idxS[s]] = (int)s;
+  }
+  marie_status st;
+  if ((st = dev_alloc(h, (void**)&h->vox2sol, nD * sizeof(int))) != MARIE_OK) return fail(st);
+  if (cudaMemcpy(h->vox2sol, vox.data(), nD * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("upload of the body map failed");
+    return fail(MARIE_ERR_CUDA);
+  }
+  if ((st = dev_alloc(h, (void**)&h->idxS, h->Ns * sizeof(int64_t))) != MARIE_OK) return fail(st);
+  cudaMemcpy(h->idxS, idxS.data(), h->Ns * sizeof(int64_t), cudaMemcpyHostToDevice);
+  // contrast chi = (1./Mr).*Mc on the body (mvp_vie.m:17)
+  std::vector<cplx<double>> chi(h->Ns);
+  for (int64_t s = 0; s < h->Ns; ++s) {
+    const std::complex<double> Mr(d->Mr[2 * idxS[s]], d->Mr[2 * idxS[s] + 1]);
+    if (!std::isfinite(Mr.real()) || !std::isfinite(Mr.imag()) || Mr == 0.0) {
+      set_error("Mr is zero or non-finite at body voxel %lld", (long long)s);
+      return fail(MARIE_ERR_NONFINITE);
+    }
+    const std::complex<double> Mc = Mr - 1.0;
+    const std::complex<double> v = (1.0 / Mr) * Mc;
+    chi[s] = cplx<double>{v.real(), v.imag()};
+  }
+  (void)e0;
+  for (int pr = 0; pr < 2; ++pr) {
+    if (!(d->precisions & (1 << pr))) continue;
+    if (pr == 0) {
+      PrecState<double>& ps = h->p64;
+      if ((st = build_axis(h, h->n1, ps.ax)) != MARIE_OK) return fail(st);
+      if ((st = build_axis(h, h->n2, ps.ay)) != MARIE_OK) return fail(st);
+      if ((st = build_axis(h, h->n3, ps.az)) != MARIE_OK) return fail(st);
+      if ((st = dev_alloc(h, (void**)&ps.chi, h->Ns * sizeof(cplx<double>))) != MARIE_OK) return fail(st);
+      cudaMemcpy(ps.chi, chi.data(), h->Ns * sizeof(cplx<double>), cudaMemcpyHostToDevice);
+      choose_tiles(h, ps);
+      if ((st = alloc_workspace(h, ps)) != MARIE_OK) return fail(st);
+    } else {
+      PrecState<float>& ps = h->p32;
+      if ((st = build_axis(h, h->n1, ps.ax)) != MARIE_OK) return fail(st);
+      if ((st = build_axis(h, h->n2, ps.ay)) != MARIE_OK) return fail(st);
+      if ((st = build_axis(h, h->n3, ps.az)) != MARIE_OK) return fail(st);
+      std::vector<cplx<float>> chif(h->Ns);
+      for (int64_t s = 0; s < h->Ns; ++s) chif[s] = cplx<float>{(float)chi[s].x, (float)chi[s].y};
+      if ((st = dev_alloc(h, (void**)&ps.chi, h->Ns * sizeof(cplx<float>))) != MARIE_OK) return fail(st);
+      cudaMemcpy(ps.chi, chif.data(), h->Ns * sizeof(cplx<float>), cudaMemcpyHostToDevice);
+      choose_tiles(h, ps);
+      if ((st = alloc_workspace(h, ps)) != MARIE_OK) return fail(st);
+    }
+  }
+  if ((st = build_spectra(h, d)) != MARIE_OK) return fail(st);
+  if (h->precisions & 1) h->p64.built = true;
+  if (h->precisions & 2) h->p32.built = true;
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_error("device error during create: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(MARIE_ERR_CUDA);
+  }
+  *out = h;
+  return MARIE_OK;
+}
+
+marie_status marie_vie_destroy(marie_vie* h) {
+  if (!h) return MARIE_OK;
+  dev_free_all(h);
+  delete h;
+  return MARIE_OK;
+}
+
+static marie_status apply_common(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream,
+                                 int mode, int op) {
+  if (!h) { set_error("handle is NULL"); return MARIE_ERR_BAD_ARG; }
+  if (!x || !y) { set_error("x or y is NULL"); return MARIE_ERR_BAD_ARG; }
+  if (nrhs < 1) { set_error("nrhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
+  if (prec != MARIE_C128 && prec != MARIE_C64) { set_error("prec must be MARIE_C128 or MARIE_C64"); return MARIE_ERR_BAD_ARG; }
+  const int64_t len = mode == MV_GRID ? (int64_t)h->C * h->n1 * h->n2 * h->n3 : h->Nb;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (prec == MARIE_C128)
+    return launch_matvec<double>(h, mode, op, (const cplx<double>*)x, len, (cplx<double>*)y, len, nrhs, nullptr, s);
+  return launch_matvec<float>(h, mode, op, (const cplx<float>*)x, len, (cplx<float>*)y, len, nrhs, nullptr, s);
+}
+
+marie_status marie_vie_apply(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_VIE, OP_N);
+}
+marie_status marie_vie_apply_adjoint(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_VIE_ADJ, OP_N_ADJ);
+}
+marie_status marie_vie_apply_N(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_GRID, OP_N);
+}
+marie_status marie_vie_apply_N_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_GRID, OP_N_ADJ);
+}
+marie_status marie_vie_apply_K(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_GRID, OP_K);
+}
+marie_status marie_vie_apply_K_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_GRID, OP_K_ADJ);
+}
+
+const char* marie_last_error(void) { return t_err.c_str(); }
+const char* marie_version(void) { return "marie_gb300 0.1 (sm_103a)"; }
+int64_t marie_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,702 @@
+// Batched restarted GMRES for the VIE operator.
+//
+// One Krylov space per right-hand side (the reference solves ports one at a
+// time, ie_solver_vie.m:16-21); all right-hand sides of a batch advance in
+// lock-step through the Arnoldi loop and a converged one simply drops out of
+// the active mask until the cycle ends.  Per cycle the arithmetic is that of
+// is_iter_gmres_vie.m:10-38: classical Gram-Schmidt in a single pass
+// (h = V^H w; w -= V h; h_{k+1,k} = ||w||), the (k+1) x k least-squares problem
+// for the residual estimate at every k, x += V y and r = V (beta e1 - H y) at
+// the end of a cycle.  The least-squares problem is solved by Givens rotations
+// in FP64 (same minimiser and residual norm as MATLAB's H \ rhs).
+//
+// Reductions are deterministic: per-CTA partials (warp shuffles + shared
+// memory), then a fixed-order FP64 sum over CTAs.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace marie {
+
+typedef cplx<double> zd;
+constexpr int kVT = 256;          // threads per vector CTA
+constexpr int kVE = 8;            // elements per thread
+constexpr int kCH = kVT * kVE;    // elements per chunk
+
+enum RhsState : int { ST_ACTIVE = 0, ST_DONE = 1, ST_MAXIT = 2, ST_NONFINITE = 3 };
+
+template <typename T>
+__device__ __forceinline__ zd to_zd(cplx<T> v) { return zd{(double)v.x, (double)v.y}; }
+
+// Block-wide sum of a complex value held by every thread; result valid in thread 0.
+template <typename A>
+__device__ __forceinline__ cplx<A> block_sum(cplx<A> v, cplx<A>* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  cplx<A> r = {0, 0};
+  if (threadIdx.x < 32) {
+    r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : cplx<A>{0, 0};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      r.x += __shfl_xor_sync(0xffffffffu, r.x, o);
+      r.y += __shfl_xor_sync(0xffffffffu, r.y, o);
+    }
+  }
+  __syncthreads();
+  return r;
+}
+
+// Accumulator type: FP32 for complex64 vectors, FP64 for complex128.
+template <typename T>
+struct Acc { typedef T type; };
+
+// part[(r*(m+1) + j)*nch + chunk] = sum_i conj(V_j[i]) w[i], j in [0, k]
+template <typename T>
+__global__ void k_dots(const cplx<T>* V, int64_t ld, int64_t Nb, int k, int mp1, const unsigned char* act,
+                       zd* part, int nch) {
+  typedef typename Acc<T>::type A;
+  __shared__ cplx<A> sh[32];
+  const int r = blockIdx.y;
+  if (!act[r]) return;
+  const int chunk = blockIdx.x;
+  const cplx<T>* base = V + (int64_t)r * mp1 * ld;
+  const cplx<T>* w = base + (int64_t)(k + 1) * ld;
+  cplx<T> wv[kVE];
+  const int64_t i0 = (int64_t)chunk * kCH + threadIdx.x;
+#pragma unroll
+  for (int e = 0; e < kVE; ++e) {
+    const int64_t i = i0 + (int64_t)e * kVT;
+    wv[e] = i < Nb ? w[i] : cplx<T>{0, 0};
+  }
+  for (int j = 0; j <= k; ++j) {
+    const cplx<T>* vj = base + (int64_t)j * ld;
+    cplx<A> acc = {0, 0};
+#pragma unroll
+    for (int e = 0; e < kVE; ++e) {
+      const int64_t i = i0 + (int64_t)e * kVT;
+      if (i < Nb) {
+        const cplx<T> v = vj[i];
+        acc.x += (A)v.x * (A)wv[e].x + (A)v.y * (A)wv[e].y;
+        acc.y += (A)v.x * (A)wv[e].y - (A)v.y * (A)wv[e].x;
+      }
+    }
+    cplx<A> s = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[((int64_t)r * mp1 + j) * nch + chunk] = zd{(double)s.x, (double)s.y};
+  }
+}
+
+// H[r][j + (m+1) k] = sum_chunk part, j in [0,k]
+__global__ void k_reduce_dots(const zd* part, int nch, int k, int mp1, int m, const unsigned char* act, zd* H) {
+  const int r = blockIdx.x;
+  if (!act[r]) return;
+  for (int j = threadIdx.x; j <= k; j += blockDim.x) {
+    const zd* p = part + ((int64_t)r * mp1 + j) * nch;
+    double sx = 0, sy = 0;
+    for (int c = 0; c < nch; ++c) { sx += p[c].x; sy += p[c].y; }
+    H[(int64_t)r * mp1 * m + j + (int64_t)mp1 * k] = zd{sx, sy};
+  }
+}
+
+// w -= sum_j V_j h_j ; npart[r*nch + chunk] = ||w_chunk||^2
+template <typename T>
+__global__ void k_update(cplx<T>* V, int64_t ld, int64_t Nb, int k, int mp1, int m, const unsigned char* act,
+                         const zd* H, double* npart, int nch) {
+  typedef typename Acc<T>::type A;
+  __shared__ cplx<T> hs[64];
+  __shared__ cplx<A> sh[32];
+  const int r = blockIdx.y;
+  if (!act[r]) return;
+  const int chunk = blockIdx.x;
+  for (int j = threadIdx.x; j <= k; j += blockDim.x) {
+    const zd hv = H[(int64_t)r * mp1 * m + j + (int64_t)mp1 * k];
+    hs[j] = cplx<T>{(T)hv.x, (T)hv.y};
+  }
+  __syncthreads();
+  cplx<T>* base = V + (int64_t)r * mp1 * ld;
+  cplx<T>* w = base + (int64_t)(k + 1) * ld;
+  const int64_t i0 = (int64_t)chunk * kCH + threadIdx.x;
+  cplx<T> wv[kVE];
+#pragma unroll
+  for (int e = 0; e < kVE; ++e) {
+    const int64_t i = i0 + (int64_t)e * kVT;
+    wv[e] = i < Nb ? w[i] : cplx<T>{0, 0};
+  }
+  for (int j = 0; j <= k; ++j) {
+    const cplx<T>* vj = base + (int64_t)j * ld;
+    const cplx<T> hj = hs[j];
+#pragma unroll
+    for (int e = 0; e < kVE; ++e) {
+      const int64_t i = i0 + (int64_t)e * kVT;
+      if (i < Nb) {
+        const cplx<T> v = vj[i];
+        wv[e].x -= v.x * hj.x - v.y * hj.y;
+        wv[e].y -= v.x * hj.y + v.y * hj.x;
+      }
+    }
+  }
+  A nrm = 0;
+#pragma unroll
+  for (int e = 0; e < kVE; ++e) {
+    const int64_t i = i0 + (int64_t)e * kVT;
+    if (i < Nb) {
+      w[i] = wv[e];
+      nrm += (A)wv[e].x * (A)wv[e].x + (A)wv[e].y * (A)wv[e].y;
+    }
+  }
+  cplx<A> s = block_sum(cplx<A>{nrm, 0}, sh);
+  if (threadIdx.x == 0) npart[(int64_t)r * nch + chunk] = (double)s.x;
+}
+
+// npart[r*nch + chunk] = ||v_r chunk||^2 for v_r = base + r*rs
+template <typename T>
+__global__ void k_norm2(const cplx<T>* v, int64_t rs, int64_t Nb, const unsigned char* act, double* npart, int nch) {
+  typedef typename Acc<T>::type A;
+  __shared__ cplx<A> sh[32];
+  const int r = blockIdx.y;
+  if (act && !act[r]) return;
+  const cplx<T>* p = v + (int64_t)r * rs;
+  const int64_t i0 = (int64_t)blockIdx.x * kCH + threadIdx.x;
+  A nrm = 0;
+#pragma unroll
+  for (int e = 0; e < kVE; ++e) {
+    const int64_t i = i0 + (int64_t)e * kVT;
+    if (i < Nb) {
+      const cplx<T> x = p[i];
+      nrm += (A)x.x * (A)x.x + (A)x.y * (A)x.y;
+    }
+  }
+  cplx<A> s = block_sum(cplx<A>{nrm, 0}, sh);
+  if (threadIdx.x == 0) npart[(int64_t)r * nch + blockIdx.x] = (double)s.x;
+}
+
+// out[r] = sqrt(sum_chunk npart)
+__global__ void k_reduce_norm(const double* npart, int nch, int nrhs, const unsigned char* act, double* out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrhs || (act && !act[r])) return;
+  double s = 0;
+  for (int c = 0; c < nch; ++c) s += npart[(int64_t)r * nch + c];
+  out[r] = sqrt(s);
+}
+
+// v_r *= 1/s_r  (zero when s_r == 0)
+template <typename T>
+__global__ void k_scale(cplx<T>* v, int64_t rs, int64_t Nb, const unsigned char* act, const double* s) {
+  const int r = blockIdx.y;
+  if (!act[r]) return;
+  const double sv = s[r];
+  const T inv = sv > 0 ? (T)(1.0 / sv) : (T)0;
+  cplx<T>* p = v + (int64_t)r * rs;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = scale(p[i], inv);
+}
+
+struct GmState {
+  zd* H;          // [nrhs][(m+1)*m]   Hessenberg (original)
+  zd* R;          // [nrhs][(m+1)*m]   rotated copy
+  double* cs;     // [nrhs][m]
+  zd* sn;         // [nrhs][m]
+  zd* g;          // [nrhs][m+1]
+  zd* y;          // [nrhs][m]
+  zd* res;        // [nrhs][m+1]
+  double* beta;   // [nrhs]
+  double* hnorm;  // [nrhs]   h_{k+1,k}
+  double* resid;  // [nrhs]   |g_{k+1}|
+  double* tolabs; // [nrhs]
+  int* kr;        // [nrhs]   Arnoldi steps in the current cycle
+  unsigned char* incyc;  // [nrhs] in the Arnoldi loop of the current cycle
+  zd* part;       // [nrhs][m+1][nch]
+  double* npart;  // [nrhs][nch]
+};
+
+// Givens step for column k (one thread per rhs).  Sets incyc=0 when the cycle
+// ends (converged, breakdown, k+1 == m or non-finite).
+__global__ void k_givens(GmState st, int k, int m, int nrhs) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrhs || !st.incyc[r]) return;
+  const int mp1 = m + 1;
+  zd* H = st.H + (int64_t)r * mp1 * m;
+  zd* R = st.R + (int64_t)r * mp1 * m;
+  double* cs = st.cs + (int64_t)r * m;
+  zd* sn = st.sn + (int64_t)r * m;
+  zd* g = st.g + (int64_t)r * mp1;
+  const double hk1 = st.hnorm[r];
+  H[k + 1 + mp1 * k] = zd{hk1, 0};
+  for (int i = 0; i <= k; ++i) R[i + mp1 * k] = H[i + mp1 * k];
+  R[k + 1 + mp1 * k] = zd{hk1, 0};
+  for (int i = 0; i < k; ++i) {
+    const zd a = R[i + mp1 * k], b = R[i + 1 + mp1 * k];
+    const double c = cs[i];
+    const zd s = sn[i];
+    R[i + mp1 * k] = zd{c * a.x + (s.x * b.x - s.y * b.y), c * a.y + (s.x * b.y + s.y * b.x)};
+    // -conj(s)*a + c*b
+    R[i + 1 + mp1 * k] = zd{-(s.x * a.x + s.y * a.y) + c * b.x, -(s.x * a.y - s.y * a.x) + c * b.y};
+  }
+  const zd a = R[k + mp1 * k];
+  const double b = hk1;
+  const double na = sqrt(a.x * a.x + a.y * a.y);
+  double c;
+  zd s;
+  if (na == 0.0) {
+    c = 0.0;
+    s = zd{1.0, 0.0};
+  } else {
+    const double t = sqrt(na * na + b * b);
+    c = na / t;
+    s = zd{a.x / na * b / t, a.y / na * b / t};
+  }
+  cs[k] = c;
+  sn[k] = s;
+  R[k + mp1 * k] = zd{c * a.x + s.x * b, c * a.y + s.y * b};
+  R[k + 1 + mp1 * k] = zd{0, 0};
+  const zd gk = g[k];
+  g[k + 1] = zd{-(s.x * gk.x + s.y * gk.y), -(s.x * gk.y - s.y * gk.x)};
+  g[k] = zd{c * gk.x, c * gk.y};
+  const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
+  st.resid[r] = res;
+  st.kr[r] = k + 1;
+  if (!isfinite(res) || !isfinite(hk1)) {
+    st.incyc[r] = 0;
+    return;
+  }
+  if (res < st.tolabs[r] || k + 1 == m || hk1 == 0.0) st.incyc[r] = 0;
+}
+
+// y = R^{-1} g (k x k), res = beta e1 - H y ((k+1) entries); one thread per rhs.
+__global__ void k_solve_y(GmState st, int m, int nrhs, const unsigned char* ran) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrhs || !ran[r]) return;
+  const int k = st.kr[r];
+  const int mp1 = m + 1;
+  const zd* H = st.H + (int64_t)r * mp1 * m;
+  const zd* R = st.R + (int64_t)r * mp1 * m;
+  const zd* g = st.g + (int64_t)r * mp1;
+  zd* y = st.y + (int64_t)r * m;
+  zd* res = st.res + (int64_t)r * mp1;
+  for (int i = k - 1; i >= 0; --i) {
+    zd acc = g[i];
+    for (int j = i + 1; j < k; ++j) acc = acc - R[i + mp1 * j] * y[j];
+    const zd d = R[i + mp1 * i];
+    const double dd = d.x * d.x + d.y * d.y;
+    y[i] = dd > 0 ? zd{(acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd} : zd{0, 0};
+  }
+  for (int i = 0; i <= k; ++i) {
+    zd acc = i == 0 ? zd{st.beta[r], 0} : zd{0, 0};
+    for (int j = 0; j < k; ++j) acc = acc - H[i + mp1 * j] * y[j];
+    res[i] = acc;
+  }
+}
+
+// x_r += sum_{j<k_r} V_j y_j   (x in FP64)
+template <typename T>
+__global__ void k_xupdate(const cplx<T>* V, int64_t ld, int mp1, int m, int64_t Nb, const unsigned char* ran,
+                          GmState st, zd* x, int64_t xrs) {
+  const int r = blockIdx.y;
+  if (!ran[r]) return;
+  const int k = st.kr[r];
+  const zd* y = st.y + (int64_t)r * m;
+  const cplx<T>* base = V + (int64_t)r * mp1 * ld;
+  zd* xr = x + (int64_t)r * xrs;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
+    zd acc = xr[i];
+    for (int j = 0; j < k; ++j) acc = acc + to_zd(base[(int64_t)j * ld + i]) * y[j];
+    xr[i] = acc;
+  }
+}
+
+// V_0 <- sum_{j<=k_r} V_j res_j  (the next cycle's residual, is_iter_gmres_vie.m:38)
+template <typename T>
+__global__ void k_rform(cplx<T>* V, int64_t ld, int mp1, int64_t Nb, const unsigned char* ran, GmState st) {
+  const int r = blockIdx.y;
+  if (!ran[r]) return;
+  const int k = st.kr[r];
+  const zd* res = st.res + (int64_t)r * mp1;
+  cplx<T>* base = V + (int64_t)r * mp1 * ld;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
+    zd acc = {0, 0};
+    for (int j = 0; j <= k; ++j) acc = acc + to_zd(base[(int64_t)j * ld + i]) * res[j];
+    base[i] = cplx<T>{(T)acc.x, (T)acc.y};
+  }
+}
+
+// Start a cycle: g = [beta, 0...]; V_0 /= beta.
+__global__ void k_cycle_init(GmState st, int m, int nrhs, const unsigned char* start) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrhs || !start[r]) return;
+  zd* g = st.g + (int64_t)r * (m + 1);
+  for (int i = 0; i <= m; ++i) g[i] = zd{0, 0};
+  g[0] = zd{st.beta[r], 0};
+  st.kr[r] = 0;
+  st.incyc[r] = 1;
+}
+
+// dst_r = (Tout) src_r
+template <typename Ti, typename To>
+__global__ void k_convert(const cplx<Ti>* src, int64_t srs, cplx<To>* dst, int64_t drs, int64_t Nb,
+                          const unsigned char* act) {
+  const int r = blockIdx.y;
+  if (act && !act[r]) return;
+  const cplx<Ti>* s = src + (int64_t)r * srs;
+  cplx<To>* d = dst + (int64_t)r * drs;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = cplx<To>{(To)s[i].x, (To)s[i].y};
+}
+
+// r = b - r  (r holds A x on entry); FP64
+__global__ void k_residual(const zd* b, zd* r, int64_t Nb, const unsigned char* act) {
+  const int k = blockIdx.y;
+  if (act && !act[k]) return;
+  const zd* bb = b + (int64_t)k * Nb;
+  zd* rr = r + (int64_t)k * Nb;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x)
+    rr[i] = bb[i] - rr[i];
+}
+
+__global__ void k_zero(zd* x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = zd{0, 0};
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+struct Scratch {
+  std::vector<void*> ptrs;
+  marie_vie* h;
+  explicit Scratch(marie_vie* hh) : h(hh) {}
+  ~Scratch() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename P>
+  marie_status get(P** p, size_t count) {
+    *p = nullptr;
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(P);
+    if (h->mem_cap > 0 && h->mem_used + (int64_t)bytes > h->mem_cap) {
+      set_error("device memory cap exceeded by GMRES workspace (%zu bytes)", bytes);
+      return MARIE_ERR_OOM;
+    }
+    if (cudaMalloc((void**)p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("GMRES workspace allocation of %zu bytes failed", bytes);
+      return MARIE_ERR_OOM;
+    }
+    ptrs.push_back(*p);
+    return MARIE_OK;
+  }
+};
+
+static dim3 vgrid(int64_t Nb, int nrhs) {
+  int64_t bx = (Nb + 255) / 256;
+  if (bx > 4096) bx = 4096;
+  return dim3((unsigned)bx, (unsigned)nrhs);
+}
+
+struct RhsLog {
+  std::vector<double> resvec;   // relative residual history
+  int iters = 0, outer = 0, last_inner = 0, status = MARIE_OK;
+};
+
+// Run restarted GMRES on A_T for all rhs with todo[r] != 0.  On entry V_0 of
+// each such rhs holds its initial residual r0 (unnormalised); bnorm[r] is the
+// reference norm for the relative tolerance.  x (FP64) receives += V y.
+template <typename T>
+static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x, const std::vector<double>& bnorm,
+                               const std::vector<double>& tolrel, int maxit, const std::vector<unsigned char>& todo,
+                               std::vector<RhsLog>& log, int* matvecs, cudaStream_t s, Scratch& sc) {
+  const int64_t Nb = h->Nb;
+  const int mp1 = m + 1;
+  const int nch = (int)((Nb + kCH - 1) / kCH);
+  GmState st;
+  MARIE_TRY(sc.get(&st.H, (size_t)nrhs * mp1 * m));
+  MARIE_TRY(sc.get(&st.R, (size_t)nrhs * mp1 * m));
+  MARIE_TRY(sc.get(&st.cs, (size_t)nrhs * m));
+  MARIE_TRY(sc.get(&st.sn, (size_t)nrhs * m));
+  MARIE_TRY(sc.get(&st.g, (size_t)nrhs * mp1));
+  MARIE_TRY(sc.get(&st.y, (size_t)nrhs * m));
+  MARIE_TRY(sc.get(&st.res, (size_t)nrhs * mp1));
+  MARIE_TRY(sc.get(&st.beta, nrhs));
+  MARIE_TRY(sc.get(&st.hnorm, nrhs));
+  MARIE_TRY(sc.get(&st.resid, nrhs));
+  MARIE_TRY(sc.get(&st.tolabs, nrhs));
+  MARIE_TRY(sc.get(&st.kr, nrhs));
+  MARIE_TRY(sc.get(&st.incyc, nrhs));
+  MARIE_TRY(sc.get(&st.part, (size_t)nrhs * mp1 * nch));
+  MARIE_TRY(sc.get(&st.npart, (size_t)nrhs * nch));
+  unsigned char* d_mask = nullptr;
+  MARIE_TRY(sc.get(&d_mask, nrhs));
+  MARIE_CUDA_TRY(cudaMemsetAsync(st.H, 0, sizeof(zd) * nrhs * mp1 * m, s));
+  std::vector<double> tolabs(nrhs);
+  for (int r = 0; r < nrhs; ++r) tolabs[r] = tolrel[r] * bnorm[r];
+  MARIE_CUDA_TRY(cudaMemcpyAsync(st.tolabs, tolabs.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, todo.data(), nrhs, cudaMemcpyHostToDevice, s));
+  const int64_t ld = Nb;
+  const int64_t vrs = (int64_t)mp1 * Nb;
+  const dim3 cg((unsigned)nch, (unsigned)nrhs);
+  const unsigned sb = (unsigned)((nrhs + 127) / 128);
+  // beta = ||r0||
+  k_norm2<T><<<cg, kVT, 0, s>>>(V, vrs, Nb, d_mask, st.npart, nch);
+  MARIE_LAUNCH_CHECK();
+  k_reduce_norm<<<sb, 128, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
+  MARIE_LAUNCH_CHECK();
+  std::vector<double> beta(nrhs, 0.0);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(beta.data(), st.beta, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<unsigned char> start(nrhs, 0);
+  int nstart = 0;
+  for (int r = 0; r < nrhs; ++r) {
+    if (!todo[r]) continue;
+    const double rel = bnorm[r] > 0 ? beta[r] / bnorm[r] : 0.0;
+    log[r].resvec.push_back(rel);
+    if (!std::isfinite(rel)) { log[r].status = MARIE_ERR_NONFINITE; continue; }
+    if (rel > tolrel[r] && maxit > 0) { start[r] = 1; ++nstart; }
+  }
+  std::vector<unsigned char> incyc(nrhs), prev(nrhs);
+  std::vector<double> resid(nrhs);
+  std::vector<int> kr(nrhs);
+  int outit = 0;
+  while (nstart > 0) {
+    ++outit;
+    MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, start.data(), nrhs, cudaMemcpyHostToDevice, s));
+    k_scale<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, vrs, Nb, d_mask, st.beta);
+    MARIE_LAUNCH_CHECK();
+    k_cycle_init<<<sb, 128, 0, s>>>(st, m, nrhs, d_mask);
+    MARIE_LAUNCH_CHECK();
+    for (int r = 0; r < nrhs; ++r) if (start[r]) log[r].outer = outit;
+    incyc = start;
+    for (int k = 0; k < m; ++k) {
+      MARIE_TRY(launch_matvec<T>(h, MV_VIE, OP_N, V + (int64_t)k * ld, vrs, V + (int64_t)(k + 1) * ld, vrs, nrhs,
+                                 st.incyc, s));
+      ++*matvecs;
+      k_dots<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, st.incyc, st.part, nch);
+      MARIE_LAUNCH_CHECK();
+      k_reduce_dots<<<nrhs, 64, 0, s>>>(st.part, nch, k, mp1, m, st.incyc, st.H);
+      MARIE_LAUNCH_CHECK();
+      k_update<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, m, st.incyc, st.H, st.npart, nch);
+      MARIE_LAUNCH_CHECK();
+      k_reduce_norm<<<sb, 128, 0, s>>>(st.npart, nch, nrhs, st.incyc, st.hnorm);
+      MARIE_LAUNCH_CHECK();
+      // scale with the mask before the Givens step clears finished rhs
+      k_scale<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V + (int64_t)(k + 1) * ld, vrs, Nb, st.incyc, st.hnorm);
+      MARIE_LAUNCH_CHECK();
+      k_givens<<<sb, 128, 0, s>>>(st, k, m, nrhs);
+      MARIE_LAUNCH_CHECK();
+      prev = incyc;
+      MARIE_CUDA_TRY(cudaMemcpyAsync(incyc.data(), st.incyc, nrhs, cudaMemcpyDeviceToHost, s));
+      MARIE_CUDA_TRY(cudaMemcpyAsync(resid.data(), st.resid, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+      MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+      int any = 0;
+      for (int r = 0; r < nrhs; ++r) {
+        if (!prev[r]) continue;
+        log[r].resvec.push_back(resid[r] / bnorm[r]);
+        log[r].iters++;
+        if (incyc[r]) any = 1;
+      }
+      if (!any) break;
+    }
+    // finalize the cycle of every rhs that ran it
+    MARIE_CUDA_TRY(cudaMemcpyAsync(kr.data(), st.kr, nrhs * sizeof(int), cudaMemcpyDeviceToHost, s));
+    MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, start.data(), nrhs, cudaMemcpyHostToDevice, s));
+    k_solve_y<<<sb, 128, 0, s>>>(st, m, nrhs, d_mask);
+    MARIE_LAUNCH_CHECK();
+    k_xupdate<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, ld, mp1, m, Nb, d_mask, st, x, Nb);
+    MARIE_LAUNCH_CHECK();
+    k_rform<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, ld, mp1, Nb, d_mask, st);
+    MARIE_LAUNCH_CHECK();
+    k_norm2<T><<<cg, kVT, 0, s>>>(V, vrs, Nb, d_mask, st.npart, nch);
+    MARIE_LAUNCH_CHECK();
+    k_reduce_norm<<<sb, 128, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
+    MARIE_LAUNCH_CHECK();
+    MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+    nstart = 0;
+    for (int r = 0; r < nrhs; ++r) {
+      if (!start[r]) continue;
+      log[r].last_inner = kr[r];
+      const double rel = log[r].resvec.back();
+      start[r] = 0;
+      if (!std::isfinite(rel)) { log[r].status = MARIE_ERR_NONFINITE; continue; }
+      if (rel > tolrel[r]) {
+        if (outit < maxit) { start[r] = 1; ++nstart; }
+        else log[r].status = MARIE_ERR_NOT_CONVERGED;
+      }
+    }
+  }
+  return MARIE_OK;
+}
+
+// r = b - A64 x for rhs in mask; returns ||r||/||b|| per rhs on the host.
+static marie_status true_residual(marie_vie* h, int nrhs, const zd* b, const zd* x, zd* r,
+                                  const std::vector<unsigned char>& mask, const std::vector<double>& bnorm,
+                                  std::vector<double>& rel, int* matvecs, cudaStream_t s, Scratch& sc) {
+  const int64_t Nb = h->Nb;
+  unsigned char* d_mask = nullptr;
+  MARIE_TRY(sc.get(&d_mask, nrhs));
+  const int nch = (int)((Nb + kCH - 1) / kCH);
+  double *npart = nullptr, *nr = nullptr;
+  MARIE_TRY(sc.get(&npart, (size_t)nrhs * nch));
+  MARIE_TRY(sc.get(&nr, nrhs));
+  MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, mask.data(), nrhs, cudaMemcpyHostToDevice, s));
+  MARIE_TRY(launch_matvec<double>(h, MV_VIE, OP_N, (const cplx<double>*)x, Nb, (cplx<double>*)r, Nb, nrhs, d_mask, s));
+  ++*matvecs;
+  k_residual<<<vgrid(Nb, nrhs), 256, 0, s>>>(b, r, Nb, d_mask);
+  MARIE_LAUNCH_CHECK();
+  k_norm2<double><<<dim3(nch, nrhs), kVT, 0, s>>>((const cplx<double>*)r, Nb, Nb, d_mask, npart, nch);
+  MARIE_LAUNCH_CHECK();
+  k_reduce_norm<<<(nrhs + 127) / 128, 128, 0, s>>>(npart, nch, nrhs, d_mask, nr);
+  MARIE_LAUNCH_CHECK();
+  std::vector<double> v(nrhs);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(v.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  rel.resize(nrhs);
+  for (int k = 0; k < nrhs; ++k)
+    if (mask[k]) rel[k] = bnorm[k] > 0 ? v[k] / bnorm[k] : 0.0;
+  return MARIE_OK;
+}
+
+static marie_status norms(marie_vie* h, int nrhs, const zd* v, std::vector<double>& out, cudaStream_t s, Scratch& sc) {
+  const int64_t Nb = h->Nb;
+  const int nch = (int)((Nb + kCH - 1) / kCH);
+  double *npart = nullptr, *nr = nullptr;
+  MARIE_TRY(sc.get(&npart, (size_t)nrhs * nch));
+  MARIE_TRY(sc.get(&nr, nrhs));
+  k_norm2<double><<<dim3(nch, nrhs), kVT, 0, s>>>((const cplx<double>*)v, Nb, Nb, nullptr, npart, nch);
+  MARIE_LAUNCH_CHECK();
+  k_reduce_norm<<<(nrhs + 127) / 128, 128, 0, s>>>(npart, nch, nrhs, nullptr, nr);
+  MARIE_LAUNCH_CHECK();
+  out.resize(nrhs);
+  MARIE_CUDA_TRY(cudaMemcpyAsync(out.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  return MARIE_OK;
+}
+
+static void fill_report(marie_gmres_report* rep, const std::vector<RhsLog>& log, const std::vector<double>& trel,
+                        int mv64, int mv32) {
+  if (!rep) return;
+  const int nrhs = (int)log.size();
+  for (int r = 0; r < nrhs; ++r) {
+    if (rep->iters) rep->iters[r] = log[r].iters;
+    if (rep->outer) rep->outer[r] = log[r].outer;
+    if (rep->last_inner) rep->last_inner[r] = log[r].last_inner;
+    if (rep->true_resid) rep->true_resid[r] = trel[r];
+    if (rep->status) rep->status[r] = log[r].status;
+    if (rep->resvec && rep->resvec_cap > 0) {
+      const int n = std::min<int>(rep->resvec_cap, (int)log[r].resvec.size());
+      for (int i = 0; i < n; ++i) rep->resvec[(int64_t)r * rep->resvec_cap + i] = log[r].resvec[i];
+      if (rep->resvec_len) rep->resvec_len[r] = n;
+    }
+  }
+  rep->matvecs_c128 = mv64;
+  rep->matvecs_c64 = mv32;
+}
+
+}  // namespace marie
+
+using namespace marie;
+
+extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, int32_t nrhs,
+                                        const marie_gmres_opts* o, marie_gmres_report* rep, void* stream) {
+  if (!h || !b_ || !x_ || !o) { set_error("NULL argument"); return MARIE_ERR_BAD_ARG; }
+  if (nrhs < 1) { set_error("nrhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
+  if (o->restart < 1 || o->restart > 64) { set_error("restart must be in [1, 64]"); return MARIE_ERR_BAD_ARG; }
+  if (o->maxit < 0) { set_error("maxit must be >= 0"); return MARIE_ERR_BAD_ARG; }
+  if (!(o->tol > 0)) { set_error("tol must be > 0"); return MARIE_ERR_BAD_ARG; }
+  if (o->mode != MARIE_SOLVE_FP64 && o->mode != MARIE_SOLVE_MIXED) { set_error("unknown solve mode"); return MARIE_ERR_BAD_ARG; }
+  if (!h->p64.built) { set_error("GMRES needs the complex128 operator (precisions bit 1)"); return MARIE_ERR_BAD_ARG; }
+  if (o->mode == MARIE_SOLVE_MIXED && !h->p32.built) { set_error("mixed mode needs the complex64 operator (precisions bit 2)"); return MARIE_ERR_BAD_ARG; }
+  cudaStream_t s = (cudaStream_t)stream;
+  const zd* b = (const zd*)b_;
+  zd* x = (zd*)x_;
+  const int64_t Nb = h->Nb;
+  const int m = o->restart;
+  Scratch sc(h);
+  std::vector<RhsLog> log(nrhs);
+  std::vector<double> bnorm;
+  MARIE_TRY(norms(h, nrhs, b, bnorm, s, sc));
+  for (int r = 0; r < nrhs; ++r)
+    if (!std::isfinite(bnorm[r])) { set_error("right-hand side %d is not finite", r); return MARIE_ERR_NONFINITE; }
+  if (!o->x0_present) {
+    k_zero<<<vgrid(Nb * nrhs, 1), 256, 0, s>>>(x, Nb * nrhs);
+    MARIE_LAUNCH_CHECK();
+  }
+  int mv64 = 0, mv32 = 0;
+  std::vector<double> trel(nrhs, 0.0);
+  std::vector<unsigned char> all(nrhs, 1);
+  zd* r64 = nullptr;
+  MARIE_TRY(sc.get(&r64, (size_t)nrhs * Nb));
+  if (o->mode == MARIE_SOLVE_FP64) {
+    cplx<double>* V = nullptr;
+    MARIE_TRY(sc.get(&V, (size_t)nrhs * (m + 1) * Nb));
+    // r0 into V_0 (is_gmres_vie.m:5-9)
+    if (o->x0_present) {
+      MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, trel, &mv64, s, sc));
+      k_convert<double, double><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)r64, Nb, V, (int64_t)(m + 1) * Nb, Nb, nullptr);
+    } else {
+      k_convert<double, double><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)b, Nb, V, (int64_t)(m + 1) * Nb, Nb, nullptr);
+    }
+    MARIE_LAUNCH_CHECK();
+    std::vector<double> tolrel(nrhs, o->tol);
+    MARIE_TRY(gmres_core<double>(h, nrhs, V, m, x, bnorm, tolrel, o->maxit, all, log, &mv64, s, sc));
+    MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, trel, &mv64, s, sc));
+  } else {
+    cplx<float>* V = nullptr;
+    MARIE_TRY(sc.get(&V, (size_t)nrhs * (m + 1) * Nb));
+    std::vector<double> rel(nrhs, 1.0);
+    if (o->x0_present) {
+      MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, rel, &mv64, s, sc));
+    } else {
+      MARIE_CUDA_TRY(cudaMemcpyAsync(r64, b, sizeof(zd) * Nb * nrhs, cudaMemcpyDeviceToDevice, s));
+      for (int r = 0; r < nrhs; ++r) rel[r] = bnorm[r] > 0 ? 1.0 : 0.0;
+    }
+    const double floor_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+    const int max_refine = o->max_refine > 0 ? o->max_refine : 10;
+    for (int it = 0; it < max_refine; ++it) {
+      std::vector<unsigned char> todo(nrhs, 0);
+      int n = 0;
+      for (int r = 0; r < nrhs; ++r)
+        if (rel[r] > o->tol && std::isfinite(rel[r]) && log[r].status == MARIE_OK) { todo[r] = 1; ++n; }
+      if (n == 0) break;
+      unsigned char* d_todo = nullptr;
+      MARIE_TRY(sc.get(&d_todo, nrhs));
+      MARIE_CUDA_TRY(cudaMemcpyAsync(d_todo, todo.data(), nrhs, cudaMemcpyHostToDevice, s));
+      k_convert<double, float><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)r64, Nb, V, (int64_t)(m + 1) * Nb, Nb, d_todo);
+      MARIE_LAUNCH_CHECK();
+      // inner problem A d = r: relative tolerance w.r.t. ||r||, asking for just
+      // enough reduction to reach the outer target (bounded by the c64 floor)
+      std::vector<double> rn(nrhs), tin(nrhs);
+      for (int r = 0; r < nrhs; ++r) {
+        rn[r] = rel[r] * bnorm[r];
+        tin[r] = std::min(0.5, std::max(floor_tol, 0.3 * o->tol / std::max(rel[r], 1e-300)));
+      }
+      std::vector<RhsLog> ilog(nrhs);
+      MARIE_TRY(gmres_core<float>(h, nrhs, V, m, x, rn, tin, o->maxit, todo, ilog, &mv32, s, sc));
+      for (int r = 0; r < nrhs; ++r) {
+        if (!todo[r]) continue;
+        log[r].iters += ilog[r].iters;
+        log[r].outer += ilog[r].outer;
+        log[r].last_inner = ilog[r].last_inner;
+        for (size_t i = 1; i < ilog[r].resvec.size(); ++i) log[r].resvec.push_back(ilog[r].resvec[i] * rel[r]);
+        if (ilog[r].status == MARIE_ERR_NONFINITE) log[r].status = MARIE_ERR_NONFINITE;
+      }
+      MARIE_TRY(true_residual(h, nrhs, b, x, r64, todo, bnorm, rel, &mv64, s, sc));
+      for (int r = 0; r < nrhs; ++r)
+        if (todo[r]) log[r].resvec.push_back(rel[r]);
+    }
+    trel = rel;
+    for (int r = 0; r < nrhs; ++r)
+      if (log[r].status == MARIE_OK && !(rel[r] <= o->tol)) log[r].status = MARIE_ERR_NOT_CONVERGED;
+  }
+  fill_report(rep, log, trel, mv64, mv32);
+  int worst = MARIE_OK;
+  for (int r = 0; r < nrhs; ++r)
+    if (log[r].status != MARIE_OK) worst = log[r].status;
+  if (worst == MARIE_ERR_NOT_CONVERGED) set_error("some right-hand sides did not reach tol");
+  if (worst == MARIE_ERR_NONFINITE) set_error("non-finite residual encountered");
+  return (marie_status)worst;
+}

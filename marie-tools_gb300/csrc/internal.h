@@ -1,0 +1,110 @@
+// Host-side runtime of the GB300 FFT-VIE library: the operator handle,
+// error reporting and the launchers shared by the translation units.
+#pragma once
+
+#include <atomic>
+#include <string>
+#include <vector>
+#include <cstdio>
+
+#include "../../include/marie_gb300.h"
+#include "matvec.cuh"
+
+namespace marie {
+
+void set_error(const char* fmt, ...);
+extern std::atomic<int64_t> g_launches;
+
+#define MARIE_CUDA_TRY(expr)                                                             \
+  do {                                                                                   \
+    cudaError_t e_ = (expr);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      ::marie::set_error("CUDA error %d (%s) at %s:%d", (int)e_, cudaGetErrorString(e_), \
+                         __FILE__, __LINE__);                                            \
+      return e_ == cudaErrorMemoryAllocation ? MARIE_ERR_OOM : MARIE_ERR_CUDA;           \
+    }                                                                                    \
+  } while (0)
+
+#define MARIE_LAUNCH_CHECK()                 \
+  do {                                       \
+    ::marie::g_launches.fetch_add(1);        \
+    MARIE_CUDA_TRY(cudaGetLastError());      \
+  } while (0)
+
+#define MARIE_TRY(expr)                \
+  do {                                 \
+    marie_status s_ = (expr);          \
+    if (s_ != MARIE_OK) return s_;     \
+  } while (0)
+
+// Device tables of one grid axis in one precision.
+template <typename T>
+struct AxisDev {
+  cplx<T>* tw = nullptr;
+  cplx<T>* tw2 = nullptr;
+  int* kofp = nullptr;
+  int* pofk = nullptr;
+  FftPlan plan{};
+};
+
+// Everything one precision of the operator needs on the device.
+template <typename T>
+struct PrecState {
+  bool built = false;
+  AxisDev<T> ax, ay, az;
+  cplx<T>* chi = nullptr;     // Ns
+  cplx<T>* GN = nullptr;      // nblkN * oct
+  cplx<T>* GK = nullptr;      // nblkK * oct
+  cplx<T>* T1 = nullptr;      // ws_rhs * C * n3 * n2 * 2n1
+  cplx<T>* S = nullptr;       // ws_rhs * C * 2n2 * n3 * 2n1
+  int ws_rhs = 0;             // right-hand sides per matvec chunk
+  int TY = 1, TXY = 1, TX = 1;
+};
+
+}  // namespace marie
+
+struct marie_vie {
+  int n1 = 0, n2 = 0, n3 = 0, C = 0, pwl = 0;
+  double res = 0, freq = 0, k0 = 0, omega = 0;
+  int64_t Ns = 0, Nb = 0;
+  int device = 0;
+  int max_rhs = 1;
+  int precisions = 0;
+  int has_K = 0;
+  int nblkN = 0, nblkK = 0;
+  int64_t mem_cap = 0, mem_used = 0;
+  double invg[12] = {0};
+  int* vox2sol = nullptr;            // device, n1*n2*n3
+  int64_t* idxS = nullptr;           // device, Ns (0-based linear voxel index)
+  std::vector<int64_t> idxS_host;
+  marie::BlockTab tab[4];            // N, N_adj, K, K_adj
+  marie::PrecState<double> p64;
+  marie::PrecState<float> p32;
+  std::vector<void*> allocs;
+  // GMRES scratch (allocated on first solve, grown on demand)
+  size_t gm_bytes = 0;
+  void* gm_base = nullptr;
+};
+
+namespace marie {
+
+marie_status dev_alloc(marie_vie* h, void** p, size_t bytes);
+void dev_free_all(marie_vie* h);
+
+enum OpKind { OP_N = 0, OP_N_ADJ = 1, OP_K = 2, OP_K_ADJ = 3 };
+
+// Enqueue one operator application on `stream`.
+//  mode: MV_GRID / MV_VIE / MV_VIE_ADJ; op: OP_*.
+//  in/out: device arrays in precision T; in_rs/out_rs: element strides between
+//  consecutive right-hand sides; active: optional per-rhs mask (device).
+template <typename T>
+marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs,
+                           cplx<T>* out, int64_t out_rs, int nrhs, const unsigned char* active,
+                           cudaStream_t stream);
+
+template <typename T>
+PrecState<T>& prec_state(marie_vie* h);
+
+marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
+
+}  // namespace marie

@@ -1,0 +1,240 @@
+// Green's-tensor spectra: one-time construction of the octant spectrum of each
+// circulant block, either from the reference's Tucker factors (the expansion
+// that mvp_N_pwl_tucker.m:31 repeats in every product) or from a dense I_V
+// block (assembly_fft_circ_tucker_pwl.m:53 without the HOSVD truncation).
+//
+// Octant spectrum: for each block, G_hat(kx,ky,kz) for kx in [0,n1], ky in
+// [0,n2], kz in [0,n3]; the remaining frequencies follow from the circulant
+// symmetry G_hat(2n-k) = s * G_hat(k) per axis (s = +-1 per block and axis,
+// see the mirror signs in BlockTab).  Layout [blk][ky][kx][kz], scaled by
+// 1/(8 n1 n2 n3) so that the inverse transforms need no normalisation.
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace marie {
+
+typedef cplx<double> zd;
+
+// out[o][k][i] = sum_j in[o][j][i] * e(j,k),  e(0,k) = 1,
+// e(j,k) = w_2n^{jk} + s * w_2n^{-jk}  (j >= 1), k in [0, n]
+__global__ void k_circ_axis(const zd* __restrict__ in, zd* __restrict__ out, int n, int s, int64_t inner,
+                            int64_t outer, const zd* __restrict__ w2n) {
+  const int64_t total = outer * (n + 1) * inner;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ii = idx % inner;
+    const int64_t r = idx / inner;
+    const int k = (int)(r % (n + 1));
+    const int64_t o = r / (n + 1);
+    const zd* src = in + o * n * inner + ii;
+    zd acc = src[0];
+    for (int j = 1; j < n; ++j) {
+      const int e = (int)(((int64_t)j * k) % (2 * n));
+      const zd w = w2n[e];
+      const zd v = src[(int64_t)j * inner];
+      // v * (w + s*conj(w))
+      const zd ws = {w.x + s * w.x, w.y - s * w.y};
+      acc = acc + v * ws;
+    }
+    out[idx] = acc;
+  }
+}
+
+// P1[a + r1(b + r2 kz)] = sum_c G[a + r1(b + r2 c)] U3[c + r3 kz]
+__global__ void k_tk1(const zd* G, const zd* U3, zd* P1, int r1, int r2, int r3, int nk) {
+  const int64_t total = (int64_t)r1 * r2 * nk;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ab = idx % ((int64_t)r1 * r2);
+    const int kz = (int)(idx / ((int64_t)r1 * r2));
+    zd acc = {0, 0};
+    for (int c = 0; c < r3; ++c) acc = acc + G[ab + (int64_t)r1 * r2 * c] * U3[c + (int64_t)r3 * kz];
+    P1[idx] = acc;
+  }
+}
+
+// P2[a + r1(ky + nky kz)] = sum_b P1[a + r1(b + r2 kz)] U2[b + r2 ky]
+__global__ void k_tk2(const zd* P1, const zd* U2, zd* P2, int r1, int r2, int nky, int nkz) {
+  const int64_t total = (int64_t)r1 * nky * nkz;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(idx % r1);
+    const int64_t r = idx / r1;
+    const int ky = (int)(r % nky);
+    const int kz = (int)(r / nky);
+    zd acc = {0, 0};
+    for (int b = 0; b < r2; ++b) acc = acc + P1[a + (int64_t)r1 * (b + (int64_t)r2 * kz)] * U2[b + (int64_t)r2 * ky];
+    P2[idx] = acc;
+  }
+}
+
+// tmp[kx + nkx(ky + nky kz)] = sum_a P2[a + r1(ky + nky kz)] U1[a + r1 kx]
+__global__ void k_tk3(const zd* P2, const zd* U1, zd* tmp, int r1, int nkx, int nky, int nkz) {
+  const int64_t total = (int64_t)nkx * nky * nkz;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(idx % nkx);
+    const int64_t yz = idx / nkx;
+    zd acc = {0, 0};
+    for (int a = 0; a < r1; ++a) acc = acc + P2[a + (int64_t)r1 * yz] * U1[a + (int64_t)r1 * kx];
+    tmp[idx] = acc;
+  }
+}
+
+// dst[(ky*nkx + kx)*nkz + kz] = scale * tmp[kx + nkx(ky + nky kz)]
+template <typename T>
+__global__ void k_oct_store(const zd* tmp, cplx<T>* dst, int nkx, int nky, int nkz, double scl) {
+  const int64_t total = (int64_t)nkx * nky * nkz;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % nkz);
+    const int64_t r = idx / nkz;
+    const int kx = (int)(r % nkx);
+    const int ky = (int)(r / nkx);
+    const zd v = tmp[kx + (int64_t)nkx * (ky + (int64_t)nky * kz)];
+    dst[idx] = cplx<T>{(T)(v.x * scl), (T)(v.y * scl)};
+  }
+}
+
+static unsigned grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 65535LL * 16) b = 65535LL * 16;
+  return (unsigned)std::max<int64_t>(1, b);
+}
+
+// Build all blocks of one operator (N or K) into the handle's spectra.
+static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const double* dense, int ncomp,
+                             cplx<double>* dst64, cplx<float>* dst32) {
+  const int n1 = h->n1, n2 = h->n2, n3 = h->n3;
+  const int pwx = h->pwl ? 10 : 1;
+  const int nblk = pwx * ncomp;
+  const int nkx = n1 + 1, nky = n2 + 1, nkz = n3 + 1;
+  const int64_t oct = (int64_t)nkx * nky * nkz;
+  const int64_t nD = (int64_t)n1 * n2 * n3;
+  const double scl = 1.0 / (8.0 * (double)n1 * (double)n2 * (double)n3);
+  // scratch
+  zd *tmp = nullptr, *a = nullptr, *b = nullptr, *w1 = nullptr, *w2 = nullptr, *w3 = nullptr;
+  zd *dG = nullptr, *dU1 = nullptr, *dU2 = nullptr, *dU3 = nullptr;
+  std::vector<void*> scratch;
+  auto salloc = [&](zd** p, size_t count) -> marie_status {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(zd));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("scratch allocation of %zu bytes failed", count * sizeof(zd));
+      return MARIE_ERR_OOM;
+    }
+    scratch.push_back(*p);
+    return MARIE_OK;
+  };
+  auto cleanup = [&]() {
+    cudaDeviceSynchronize();
+    for (void* p : scratch) cudaFree(p);
+  };
+  marie_status st = MARIE_OK;
+  const int tabk = ncomp == 6 ? 0 : 2;   // N or K table (mirror signs)
+  const BlockTab& bt = h->tab[tabk];
+  do {
+    if ((st = salloc(&tmp, oct)) != MARIE_OK) break;
+    if (dense) {
+      if ((st = salloc(&a, nD)) != MARIE_OK) break;
+      if ((st = salloc(&b, (int64_t)nkx * nky * n3)) != MARIE_OK) break;
+      // w_2n tables per axis
+      zd* ws[3] = {nullptr, nullptr, nullptr};
+      const int ns[3] = {n1, n2, n3};
+      for (int d = 0; d < 3 && st == MARIE_OK; ++d) {
+        if ((st = salloc(&ws[d], 2 * ns[d])) != MARIE_OK) break;
+        std::vector<zd> w(2 * ns[d]);
+        for (int k = 0; k < 2 * ns[d]; ++k) {
+          const long double ang = -3.141592653589793238462643383279502884L * (long double)k / (long double)ns[d];
+          w[k] = zd{(double)std::cos(ang), (double)std::sin(ang)};
+        }
+        cudaMemcpy(ws[d], w.data(), 2 * ns[d] * sizeof(zd), cudaMemcpyHostToDevice);
+      }
+      if (st != MARIE_OK) break;
+      w1 = ws[0]; w2 = ws[1]; w3 = ws[2];
+      zd* c = nullptr;
+      if ((st = salloc(&c, (int64_t)nkx * nky * n3)) != MARIE_OK) break;
+      for (int id = 0; id < nblk; ++id) {
+        // dense I_V is (n1,n2,n3,pwx,ncomp) column-major: block (j,k) at (j + pwx*k)*nD
+        const int j = id / ncomp, k = id % ncomp;
+        const double* src = dense + 2 * ((int64_t)(j + pwx * k) * nD);
+        if (cudaMemcpy(a, src, nD * sizeof(zd), cudaMemcpyHostToDevice) != cudaSuccess) {
+          set_error("upload of dense I_V failed");
+          st = MARIE_ERR_CUDA;
+          break;
+        }
+        k_circ_axis<<<grid_for((int64_t)nkx * n2 * n3), 256>>>(a, b, n1, bt.s1[id], 1, (int64_t)n2 * n3, w1);
+        g_launches++;
+        k_circ_axis<<<grid_for((int64_t)nkx * nky * n3), 256>>>(b, c, n2, bt.s2[id], nkx, n3, w2);
+        g_launches++;
+        k_circ_axis<<<grid_for(oct), 256>>>(c, tmp, n3, bt.s3[id], (int64_t)nkx * nky, 1, w3);
+        g_launches++;
+        if (dst64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        if (dst32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        if (cudaGetLastError() != cudaSuccess) { set_error("spectrum kernel launch failed"); st = MARIE_ERR_CUDA; break; }
+        cudaDeviceSynchronize();
+      }
+    } else {
+      int mr1 = 1, mr2 = 1, mr3 = 1;
+      int64_t mg = 1, mp1 = 1, mp2 = 1;
+      for (int id = 0; id < nblk; ++id) {
+        const marie_tucker_block& t = tk[id];
+        if (t.r1 < 1 || t.r2 < 1 || t.r3 < 1 || !t.G || !t.U1 || !t.U2 || !t.U3) {
+          set_error("Tucker block %d is incomplete", id);
+          st = MARIE_ERR_BAD_ARG;
+          break;
+        }
+        mr1 = std::max(mr1, t.r1); mr2 = std::max(mr2, t.r2); mr3 = std::max(mr3, t.r3);
+        mg = std::max<int64_t>(mg, (int64_t)t.r1 * t.r2 * t.r3);
+        mp1 = std::max<int64_t>(mp1, (int64_t)t.r1 * t.r2 * nkz);
+        mp2 = std::max<int64_t>(mp2, (int64_t)t.r1 * nky * nkz);
+      }
+      if (st != MARIE_OK) break;
+      if ((st = salloc(&dG, mg)) != MARIE_OK) break;
+      if ((st = salloc(&dU1, (int64_t)mr1 * 2 * n1)) != MARIE_OK) break;
+      if ((st = salloc(&dU2, (int64_t)mr2 * 2 * n2)) != MARIE_OK) break;
+      if ((st = salloc(&dU3, (int64_t)mr3 * 2 * n3)) != MARIE_OK) break;
+      if ((st = salloc(&a, mp1)) != MARIE_OK) break;
+      if ((st = salloc(&b, mp2)) != MARIE_OK) break;
+      for (int id = 0; id < nblk; ++id) {
+        const marie_tucker_block& t = tk[id];
+        cudaMemcpy(dG, t.G, (size_t)t.r1 * t.r2 * t.r3 * sizeof(zd), cudaMemcpyHostToDevice);
+        cudaMemcpy(dU1, t.U1, (size_t)t.r1 * 2 * n1 * sizeof(zd), cudaMemcpyHostToDevice);
+        cudaMemcpy(dU2, t.U2, (size_t)t.r2 * 2 * n2 * sizeof(zd), cudaMemcpyHostToDevice);
+        cudaMemcpy(dU3, t.U3, (size_t)t.r3 * 2 * n3 * sizeof(zd), cudaMemcpyHostToDevice);
+        k_tk1<<<grid_for((int64_t)t.r1 * t.r2 * nkz), 256>>>(dG, dU3, a, t.r1, t.r2, t.r3, nkz);
+        g_launches++;
+        k_tk2<<<grid_for((int64_t)t.r1 * nky * nkz), 256>>>(a, dU2, b, t.r1, t.r2, nky, nkz);
+        g_launches++;
+        k_tk3<<<grid_for(oct), 256>>>(b, dU1, tmp, t.r1, nkx, nky, nkz);
+        g_launches++;
+        if (dst64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        if (dst32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        if (cudaGetLastError() != cudaSuccess) { set_error("spectrum kernel launch failed"); st = MARIE_ERR_CUDA; break; }
+        cudaDeviceSynchronize();
+      }
+    }
+  } while (0);
+  cleanup();
+  return st;
+}
+
+marie_status build_spectra(marie_vie* h, const marie_vie_desc* d) {
+  const int64_t oct = (int64_t)(h->n1 + 1) * (h->n2 + 1) * (h->n3 + 1);
+  if (h->precisions & 1) {
+    MARIE_TRY(dev_alloc(h, (void**)&h->p64.GN, (size_t)h->nblkN * oct * sizeof(cplx<double>)));
+    if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->p64.GK, (size_t)h->nblkK * oct * sizeof(cplx<double>)));
+  }
+  if (h->precisions & 2) {
+    MARIE_TRY(dev_alloc(h, (void**)&h->p32.GN, (size_t)h->nblkN * oct * sizeof(cplx<float>)));
+    if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->p32.GK, (size_t)h->nblkK * oct * sizeof(cplx<float>)));
+  }
+  MARIE_TRY(build_op(h, d->tucker_N, d->tucker_N ? nullptr : d->dense_N, 6, h->p64.GN, h->p32.GN));
+  if (h->has_K) MARIE_TRY(build_op(h, d->tucker_K, d->tucker_K ? nullptr : d->dense_K, 3, h->p64.GK, h->p32.GK));
+  return MARIE_OK;
+}
+
+}  // namespace marie

@@ -1,0 +1,218 @@
+"""VieOperator: a handle on the GB300 FFT-VIE operator (libmarie_gb300.so).
+
+Device memory is plain ``torch`` CUDA tensors (plumbing only); every operator
+application and solve runs in the library's CUDA kernels.  Grids are flat
+column-major (x fastest) vectors of length n1*n2*n3*C per right-hand side;
+body vectors have length N_b = C*N_s in idx_solution order.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import C128, C64, PWC, PWL, SOLVE_FP64, SOLVE_MIXED, check
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_lib.c_double_p)
+
+
+def _cplx_f(a) -> np.ndarray:
+    """Complex128 array in column-major order, viewed as interleaved doubles."""
+    a = np.asarray(a, dtype=np.complex128)
+    return np.ascontiguousarray(a.reshape(-1, order="F")).view(np.float64)
+
+
+@dataclass
+class SolveReport:
+    iters: np.ndarray
+    outer: np.ndarray
+    last_inner: np.ndarray
+    true_resid: np.ndarray
+    resvec: list
+    status: np.ndarray
+    matvecs_c128: int
+    matvecs_c64: int
+    ok: bool = field(default=True)
+
+
+class VieOperator:
+    """Operator handle: body map, contrast, Green's-tensor spectra, workspaces.
+
+    Parameters mirror the reference's operator data: grid edges, basis
+    (PWC/PWL), voxel edge ``res``, frequency, ``idx_solution`` (0-based,
+    component-major), the relative permittivity map ``Mr`` (em_assembly.m:14)
+    and the N (and optionally K) operator either as Tucker blocks
+    {(j, k): (G, U1, U2, U3)} (assembly_fft_circ_tucker_*.m output) or as a
+    dense I_V array (n1, n2, n3, pwx, 6|3).
+    """
+
+    def __init__(self, dims, res, freq, idx_solution, Mr, N, K=None, *, pwl: bool,
+                 precisions: int = 3, max_rhs: int = 1, mem_cap_bytes: int = 0):
+        self._lib = _lib.load()
+        self.n1, self.n2, self.n3 = (int(v) for v in dims)
+        self.pwl = bool(pwl)
+        self.C = 12 if self.pwl else 3
+        self.res, self.freq = float(res), float(freq)
+        idx = np.ascontiguousarray(np.asarray(idx_solution, dtype=np.int64))
+        self.Nb = int(idx.size)
+        self.Ns = self.Nb // self.C
+        self.nD = self.n1 * self.n2 * self.n3
+        self._keep = []          # host arrays that must outlive create()
+        d = _lib.VieDesc()
+        d.n1, d.n2, d.n3 = self.n1, self.n2, self.n3
+        d.basis = PWL if self.pwl else PWC
+        d.res, d.freq = self.res, self.freq
+        d.n_b = self.Nb
+        d.idx_solution = idx.ctypes.data_as(ct.POINTER(ct.c_int64))
+        mr = _cplx_f(np.asarray(Mr).reshape(self.n1, self.n2, self.n3, order="F"))
+        d.Mr = _dptr(mr)
+        self._keep += [idx, mr]
+        tN, dN = self._op_arg(N, 6)
+        d.tucker_N, d.dense_N = tN, dN
+        if K is not None:
+            tK, dK = self._op_arg(K, 3)
+            d.tucker_K, d.dense_K = tK, dK
+        d.precisions, d.max_rhs, d.mem_cap_bytes = int(precisions), int(max_rhs), int(mem_cap_bytes)
+        h = ct.c_void_p()
+        check(self._lib.marie_vie_create(ct.byref(h), ct.byref(d)))
+        self._h = h
+        self._keep = None
+        self.precisions = precisions
+
+    def _op_arg(self, op, ncomp):
+        pwx = 10 if self.pwl else 1
+        if isinstance(op, dict):
+            arr = (_lib.TuckerBlock * (pwx * ncomp))()
+            for j in range(pwx):
+                for k in range(ncomp):
+                    G, U1, U2, U3 = op[(j, k)]
+                    t = arr[j * ncomp + k]
+                    t.r1, t.r2, t.r3 = G.shape
+                    bufs = [_cplx_f(G), _cplx_f(U1), _cplx_f(U2), _cplx_f(U3)]
+                    self._keep += bufs
+                    t.G, t.U1, t.U2, t.U3 = (_dptr(b) for b in bufs)
+            self._keep.append(arr)
+            return ct.cast(arr, ct.POINTER(_lib.TuckerBlock)), None
+        A = np.asarray(op)
+        if A.shape != (self.n1, self.n2, self.n3, pwx, ncomp) and not (
+                not self.pwl and A.shape == (self.n1, self.n2, self.n3, ncomp)):
+            raise ValueError(f"dense operator has shape {A.shape}")
+        buf = _cplx_f(A)
+        self._keep.append(buf)
+        return None, _dptr(buf)
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.marie_vie_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- applications -------------------------------------------------------
+    @staticmethod
+    def _stream():
+        import torch
+        return ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def _apply(self, fn, x, length, out=None):
+        import torch
+        if x.device.type != "cuda":
+            raise ValueError("x must be a CUDA tensor")
+        prec = C128 if x.dtype == torch.complex128 else (C64 if x.dtype == torch.complex64 else None)
+        if prec is None:
+            raise ValueError("x must be complex64 or complex128")
+        x = x.contiguous()
+        if x.numel() % length:
+            raise ValueError(f"x length {x.numel()} is not a multiple of {length}")
+        nrhs = x.numel() // length
+        y = torch.empty_like(x) if out is None else out
+        check(fn(self._h, prec, ct.c_void_p(x.data_ptr()), ct.c_void_p(y.data_ptr()), nrhs, self._stream()))
+        return y
+
+    def apply(self, x, out=None):
+        """mvp_vie (mvp_vie.m:1-19) on body vectors."""
+        return self._apply(self._lib.marie_vie_apply, x, self.Nb, out)
+
+    def apply_adjoint(self, x, out=None):
+        return self._apply(self._lib.marie_vie_apply_adjoint, x, self.Nb, out)
+
+    def apply_N(self, x, out=None):
+        return self._apply(self._lib.marie_vie_apply_N, x, self.C * self.nD, out)
+
+    def apply_N_adj(self, x, out=None):
+        return self._apply(self._lib.marie_vie_apply_N_adj, x, self.C * self.nD, out)
+
+    def apply_K(self, x, out=None):
+        return self._apply(self._lib.marie_vie_apply_K, x, self.C * self.nD, out)
+
+    def apply_K_adj(self, x, out=None):
+        return self._apply(self._lib.marie_vie_apply_K_adj, x, self.C * self.nD, out)
+
+    # -- solve ----------------------------------------------------------------
+    def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-5,
+              max_refine=10, resvec_cap=4096, raise_on_fail=False):
+        """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA."""
+        import torch
+        b = b.contiguous()
+        if b.dtype != torch.complex128 or b.device.type != "cuda":
+            raise ValueError("b must be a complex128 CUDA tensor")
+        nrhs = b.numel() // self.Nb
+        x0 = x is not None
+        if x is None:
+            x = torch.zeros_like(b)
+        o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol,
+                           mode=SOLVE_MIXED if mode == "mixed" else SOLVE_FP64,
+                           x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine)
+        it = np.zeros(nrhs, np.int32); ou = np.zeros(nrhs, np.int32); li = np.zeros(nrhs, np.int32)
+        tr = np.zeros(nrhs, np.float64); st = np.zeros(nrhs, np.int32); rl = np.zeros(nrhs, np.int32)
+        rv = np.zeros((nrhs, resvec_cap), np.float64)
+        ip = lambda a: a.ctypes.data_as(_lib.c_int32_p)
+        rep = _lib.GmresReport(iters=ip(it), outer=ip(ou), last_inner=ip(li), true_resid=_dptr(tr),
+                               resvec=_dptr(rv), resvec_cap=resvec_cap, resvec_len=ip(rl), status=ip(st))
+        s = self._lib.marie_gmres_vie(self._h, ct.c_void_p(b.data_ptr()), ct.c_void_p(x.data_ptr()), nrhs,
+                                      ct.byref(o), ct.byref(rep), self._stream())
+        if s not in (0, 4) or (raise_on_fail and s != 0):
+            check(s)
+        report = SolveReport(it, ou, li, tr, [rv[r, :rl[r]].copy() for r in range(nrhs)], st,
+                             rep.matvecs_c128, rep.matvecs_c64, ok=(s == 0))
+        return x, report
+
+    # -- right-hand sides -----------------------------------------------------
+    def incident_loops(self, origin, loops, radius, nseg=64):
+        """Loop incident fields tested onto the basis: (nloop*N_b) complex128 CUDA."""
+        import torch
+        loops = np.ascontiguousarray(np.asarray(loops, dtype=np.float64).reshape(-1, 6))
+        org = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))
+        out = torch.empty(loops.shape[0] * self.Nb, dtype=torch.complex128, device="cuda")
+        check(self._lib.marie_incident_loops(self._h, _dptr(org), _dptr(loops), loops.shape[0], float(radius),
+                                             int(nseg), ct.c_void_p(out.data_ptr()), self._stream()))
+        return out
+
+    def incident_plane_wave(self, origin):
+        import torch
+        org = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))
+        out = torch.empty(self.Nb, dtype=torch.complex128, device="cuda")
+        check(self._lib.marie_incident_plane_wave(self._h, _dptr(org), ct.c_void_p(out.data_ptr()),
+                                                  self._stream()))
+        return out
+
+
+def assemble_green(dims, res, freq, pwl: bool, kernel: str = "N") -> np.ndarray:
+    """I_V (n1,n2,n3,pwx,6|3) computed on the GPU (assembly_N.m / assembly_K.m)."""
+    lib = _lib.load()
+    n1, n2, n3 = (int(v) for v in dims)
+    pwx = 10 if pwl else 1
+    nc = 6 if kernel == "N" else 3
+    out = np.empty(n1 * n2 * n3 * pwx * nc * 2, dtype=np.float64)
+    check(lib.marie_assemble_green(n1, n2, n3, float(res), float(freq), PWL if pwl else PWC,
+                                   0 if kernel == "N" else 1, _dptr(out)))
+    return out.view(np.complex128).reshape((n1, n2, n3, pwx, nc), order="F")

@@ -1,0 +1,164 @@
+"""Mirror of MARIE's VIE operator/solver call surface on the GB300 library.
+
+The reference builds a table of function handles (parse_inputs.m:6-37) and
+calls them from its solver driver:
+
+    func.mvp_N(Jin, fN), func.mvp_K, func.mvp_herm_adj_N/K, func.mvp_G(T,res),
+    func.mvp_invG(T,res)
+    Jout = mvp_vie(Jb, EP, func, dim, fN)                    (mvp_vie.m:1)
+    [x, iter, resvec] = is_gmres_vie(A, b, restart, tol, maxit, x0)
+                                                            (is_gmres_vie.m:1)
+    [Jb, ...] = ie_solver_vie(MREDM, gpu_flag)               (ie_solver_vie.m:1)
+
+Here the same names take the same arguments, with ``fN`` a
+:class:`VieOperator` (the operator handle that replaces ``to_GPU(N)``) and
+arrays as CUDA tensors (gpuArray) or numpy arrays (host double); outputs
+follow the input, like MATLAB's ``'like'``.  Grids are (n1, n2, n3, C) arrays
+in MATLAB (column-major) order.  Errors raise ``MarieError`` (the reference
+raises MATLAB errors); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .operator import VieOperator
+
+
+def _to_cuda(a, dtype=None):
+    import torch
+    if isinstance(a, torch.Tensor):
+        t = a
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.complex128)))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.to("cuda")
+
+
+def _grid_flat(Jin):
+    """(n1,n2,n3,C) MATLAB-ordered array -> flat column-major CUDA vector."""
+    import torch
+    if isinstance(Jin, torch.Tensor):
+        t = Jin.permute(*reversed(range(Jin.dim()))).contiguous().reshape(-1)
+        return t.to("cuda"), Jin.shape, True
+    a = np.asarray(Jin)
+    return _to_cuda(a.reshape(-1, order="F")), a.shape, False
+
+
+def _grid_back(y, shape, was_torch, like):
+    if was_torch:
+        return y.reshape(tuple(reversed(shape))).permute(*reversed(range(len(shape)))).to(like.device)
+    return y.cpu().numpy().reshape(shape, order="F")
+
+
+def _grid_op(name):
+    def fn(Jin, fN: VieOperator):
+        flat, shape, was_torch = _grid_flat(Jin)
+        y = getattr(fN, name)(flat)
+        return _grid_back(y, shape, was_torch, Jin)
+    fn.__name__ = name
+    return fn
+
+
+mvp_N = _grid_op("apply_N")
+mvp_K = _grid_op("apply_K")
+mvp_herm_adj_N = _grid_op("apply_N_adj")
+mvp_herm_adj_K = _grid_op("apply_K_adj")
+
+
+def _gram(pwl, res):
+    if not pwl:
+        return np.full(3, res ** 3)
+    return np.tile(np.array([res ** 3, res ** 3 / 12, res ** 3 / 12, res ** 3 / 12]), 3)
+
+
+def mvp_G_pwc(T, res):
+    """mvp_G_pwc.m:3."""
+    return res ** 3 * T
+
+
+def mvp_invG_pwc(T, res):
+    """mvp_invG_pwc.m:3."""
+    return (1 / res ** 3) * T
+
+
+def mvp_G_pwl(T, res):
+    """mvp_G_pwl.m:5-9: per-component Gram diagonal on (n1,n2,n3,12)."""
+    return T * _gram(True, res).reshape((1,) * (T.ndim - 1) + (-1,))
+
+
+def mvp_invG_pwl(T, res):
+    """mvp_invG_pwl.m:3-7."""
+    return T / _gram(True, res).reshape((1,) * (T.ndim - 1) + (-1,))
+
+
+def parse_inputs(PWX: int) -> dict:
+    """The VIE entries of the function-handle table of parse_inputs.m:6-37."""
+    pwl = PWX == 1
+    return dict(mvp_N=mvp_N, mvp_K=mvp_K, mvp_herm_adj_N=mvp_herm_adj_N, mvp_herm_adj_K=mvp_herm_adj_K,
+                mvp_G=mvp_G_pwl if pwl else mvp_G_pwc, mvp_invG=mvp_invG_pwl if pwl else mvp_invG_pwc,
+                ie_solver_wsvie=ie_solver_vie)
+
+
+def mvp_vie(Jb, EP, func, dim, fN: VieOperator):
+    """Jout = Jp - (Mc./Mr) .* invG(N Jp) on the body (mvp_vie.m:1-19).
+
+    EP and dim are accepted for signature parity; the contrast and index map
+    were bound into ``fN`` when it was created, and dim['N_b'] is checked.
+    """
+    import torch
+    if dim is not None and int(dim.get("N_b", fN.Nb)) != fN.Nb:
+        raise ValueError("dim.N_b does not match the operator handle")
+    was_torch = isinstance(Jb, torch.Tensor)
+    x = _to_cuda(Jb)
+    if x.dtype not in (torch.complex64, torch.complex128):
+        x = x.to(torch.complex128)
+    y = fN.apply(x.reshape(-1)).reshape(x.shape)
+    return y if was_torch else y.cpu().numpy()
+
+
+def is_gmres_vie(A, b, restart, tol, maxit, x0, mode="fp64"):
+    """[x, iter, resvec] = is_gmres_vie(A, b, restart, tol, maxit, x0).
+
+    ``A`` is the operator handle (the reference passes the closure
+    @(J) mvp_vie(J, EP, func, dims, fN), ie_solver_vie.m:15); ``b`` may hold
+    several right-hand sides as columns (N_b x nrhs), solved in one batch.
+    Returns x (like b), iter = [p, outit] per rhs and the relative residual
+    history (a list per rhs, or one array for a single rhs).
+    """
+    import torch
+    if not isinstance(A, VieOperator):
+        raise TypeError("A must be a VieOperator (the GPU operator handle)")
+    was_torch = isinstance(b, torch.Tensor)
+    bb = _to_cuda(b, torch.complex128)
+    single = bb.dim() == 1
+    B = bb.reshape(A.Nb, -1) if not single else bb.reshape(A.Nb, 1)
+    nrhs = B.shape[1]
+    Bc = B.t().contiguous().reshape(-1)      # rhs-major for the C ABI
+    X0 = None
+    if x0 is not None:
+        xx = _to_cuda(x0, torch.complex128).reshape(A.Nb, nrhs)
+        if torch.count_nonzero(xx) > 0:
+            X0 = xx.t().contiguous().reshape(-1)
+    x, rep = A.gmres(Bc, X0, restart=restart, tol=tol, maxit=maxit, mode=mode)
+    X = x.reshape(nrhs, A.Nb).t()
+    it = np.stack([rep.last_inner, rep.outer], axis=1)
+    if single:
+        X = X.reshape(-1)
+        it, resvec = it[0], rep.resvec[0]
+    else:
+        resvec = rep.resvec
+    return (X if was_torch else X.cpu().numpy()), it, resvec
+
+
+def ie_solver_vie(fN: VieOperator, Ue, ce, Mr, Mc, idxS, tol, restart=50, maxit=200, mode="fp64"):
+    """Solver driver of ie_solver_vie.m:14-21 with the port loop batched:
+    rhs = ce * repmat((1./Mr(idxS)).*Mc(idxS), ql, 1) .* Ue(:, i) for all i."""
+    import torch
+    ql = fN.C
+    mr = np.asarray(Mr).reshape(-1, order="F")[idxS]
+    mc = np.asarray(Mc).reshape(-1, order="F")[idxS]
+    chi = np.tile((1.0 / mr) * mc, ql)
+    U = _to_cuda(Ue, torch.complex128).reshape(fN.Nb, -1)
+    rhs = ce * _to_cuda(chi, torch.complex128)[:, None] * U
+    return is_gmres_vie(fN, rhs, restart, tol, maxit, None, mode=mode)

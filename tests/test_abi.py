@@ -1,0 +1,101 @@
+"""CPU checks of the C ABI: the library builds, loads, exports every symbol the
+header declares, and rejects invalid descriptors before touching the GPU."""
+import ctypes as ct
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from marie_gb300 import _lib, _build
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return _lib.load()
+
+
+def test_exports_every_header_symbol(lib):
+    syms = _lib.header_symbols()
+    assert len(syms) >= 15
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.lib_path())], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    for s in syms:
+        assert hasattr(lib, s)
+
+
+def test_version_and_counter(lib):
+    assert b"sm_103a" in lib.marie_version()
+    assert lib.marie_launch_count() >= 0
+
+
+def _desc(**kw):
+    d = _lib.VieDesc()
+    d.n1 = d.n2 = d.n3 = 4
+    d.basis = _lib.PWC
+    d.res, d.freq = 5e-3, 128e6
+    d.precisions, d.max_rhs = 3, 1
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def _create(lib, d):
+    h = ct.c_void_p()
+    st = lib.marie_vie_create(ct.byref(h), ct.byref(d))
+    return st, h
+
+
+def test_rejects_bad_descriptors(lib):
+    idx = np.arange(3 * 5, dtype=np.int64)   # not component-major for a 4^3 grid
+    mr = np.ones(2 * 64)
+    dense = np.zeros(2 * 64 * 6)
+    base = dict(n_b=15, idx_solution=idx.ctypes.data_as(ct.POINTER(ct.c_int64)),
+                Mr=mr.ctypes.data_as(_lib.c_double_p), dense_N=dense.ctypes.data_as(_lib.c_double_p))
+    cases = [
+        dict(base, n1=0),
+        dict(base, basis=5),
+        dict(base, res=-1.0),
+        dict(base, freq=0.0),
+        dict(base, precisions=0),
+        dict(base, max_rhs=0),
+        dict(base, n_b=16),                      # not a multiple of 3
+        dict(base),                              # idx_solution not component-major
+        dict(base, dense_N=None),                # no operator
+    ]
+    for kw in cases:
+        st, h = _create(lib, _desc(**kw))
+        assert st == 1, (kw.keys(), st, _lib.last_error())
+        assert not h.value
+        assert _lib.last_error()
+
+
+def test_rejects_out_of_grid_index(lib):
+    Ns = 5
+    idxS = np.array([0, 1, 2, 3, 64], dtype=np.int64)      # 64 is outside a 4^3 grid
+    idx = np.concatenate([idxS + c * 64 for c in range(3)])
+    mr = np.ones(2 * 64)
+    dense = np.zeros(2 * 64 * 6)
+    d = _desc(n_b=3 * Ns, idx_solution=idx.ctypes.data_as(ct.POINTER(ct.c_int64)),
+              Mr=mr.ctypes.data_as(_lib.c_double_p), dense_N=dense.ctypes.data_as(_lib.c_double_p))
+    st, h = _create(lib, d)
+    assert st == 1 and "outside" in _lib.last_error()
+
+
+def test_null_handle_calls(lib):
+    assert lib.marie_vie_apply(None, 0, None, None, 1, None) == 1
+    assert lib.marie_gmres_vie(None, None, None, 1, None, None, None) == 1
+    assert lib.marie_vie_destroy(None) == 0
+
+
+def test_header_compiles_as_c(tmp_path):
+    src = tmp_path / "t.c"
+    src.write_text('#include "marie_gb300.h"\nint main(void){marie_vie_desc d; (void)d; return 0;}\n')
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-c", str(src),
+                        "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
