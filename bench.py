@@ -1,0 +1,327 @@
+"""Benchmark: batched GMRES solves of the FFT-VIE system on one GB300.
+
+Workload (default): ellipsoid phantom on a 128^3 grid at 2 mm, PWL basis
+(12 unknowns/voxel), 297.2 MHz, 64 right-hand sides from 64 loop ports on a
+16 cm cylinder; complex64 GMRES(50) with FP32 accumulation inside an FP64
+iterative-refinement loop to 1e-6 relative residual.  One step = one batched
+solve of all right-hand sides, inputs resident in HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank solves its own batch (replicas of the workload with
+rank-seeded loop jitter; no collective on the data path), value = solves of
+all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path[:0] = [str(ROOT), str(ROOT / "marie-tools_gb300")]
+
+WORKLOADS = {
+    "cfg3": dict(n=128, res=2e-3, freq=297.2e6, pwl=True, nrhs=64, tol=1e-6, phantom="ellipsoid",
+                 desc="ellipsoid phantom 128^3 @ 2 mm, PWL, 297.2 MHz, 64 loop-port RHS"),
+    "cfg2": dict(n=96, res=2e-3, freq=297.2e6, pwl=True, nrhs=1, tol=1e-6, phantom="ellipsoid",
+                 desc="ellipsoid phantom 96^3 @ 2 mm, PWL, 297.2 MHz, 1 loop RHS"),
+    "cfg1": dict(n=32, res=5e-3, freq=128e6, pwl=False, nrhs=1, tol=1e-6, phantom="sphere",
+                 desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
+}
+METRIC = "GMRES solves/s at 128^3 PWL, 1e-6 resid (mixed c64/FP64-refined, 64-RHS batch)"
+# Mean FP64 GMRES(50) iterations per right-hand side to 1e-6 on the cfg3
+# workload, measured by this library's complex128 solver (same algorithm as
+# is_gmres_vie.m); used to turn the reference arm's per-iteration time into
+# solves/s.  Updated from the 'fp64_iters_per_solve' field of our own arm.
+FP64_ITERS_CFG3 = 60.0
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_problem(wl, rank, torch):
+    """Phantom, GPU-assembled operator and right-hand sides of one workload."""
+    from marie_gb300 import VieOperator, assemble_green, phantoms
+    n, res, freq, pwl = wl["n"], wl["res"], wl["freq"], wl["pwl"]
+    if wl["phantom"] == "sphere":
+        body = phantoms.sphere(n, res, 0.06, 50.0, 0.6)
+    else:
+        body = phantoms.ellipsoid_phantom(n, res, seed=0)
+    emc = phantoms.em_constants(freq)
+    t0 = time.time()
+    ivN = assemble_green(body.n, res, freq, pwl, "N")
+    t_asm = time.time() - t0
+    op = VieOperator(body.n, res, freq, body.idx_solution(pwl), body.Mr(freq), ivN, pwl=pwl, precisions=3,
+                     max_rhs=wl["nrhs"])
+    del ivN
+    if wl["phantom"] == "sphere":
+        Ue = op.incident_plane_wave(body.origin).reshape(1, -1).repeat(wl["nrhs"], 1)
+    elif wl["nrhs"] == 1:
+        loops, radius = phantoms.loop_outside((0.080, 0.065, 0.090), gap=0.01, radius=0.05)
+        Ue = op.incident_loops(body.origin, loops, radius, nseg=64).reshape(1, -1)
+    else:
+        loops = phantoms.loop_ring(wl["nrhs"], ring_radius=0.16, seed=1 + rank)
+        Ue = op.incident_loops(body.origin, loops, 0.025, nseg=64).reshape(wl["nrhs"], -1)
+    Mr = body.Mr(freq).reshape(-1, order="F")[body.idxS]
+    chi = np.tile((1.0 / Mr) * (Mr - 1.0), 12 if pwl else 3)
+    b = (emc["ce"] * torch.from_numpy(chi).cuda()[None, :] * Ue).contiguous()   # ie_solver_vie.m:18
+    return op, body, b.reshape(-1), t_asm
+
+
+def roofline_z(op, wl, tiles, ms_z, peak, peak_kind):
+    """Algorithmic bytes of one z-pass launch / its event-timed duration."""
+    n, C = wl["n"], 12 if wl["pwl"] else 3
+    U = 60 if wl["pwl"] else 6
+    s = 8                                   # complex64
+    units = min(tiles["chunk"], wl["nrhs"])  # right-hand sides per launch
+    per_rhs = 8 * n ** 3 * C * s            # read + write 4 n^3 per component
+    green = U * (n + 1) ** 3 * s            # octant spectrum, read once per launch
+    alg = units * per_rhs + green
+    achieved = alg / (ms_z * 1e-3) / 1e9
+    # ncu dram bytes per right-hand side of one z-pass launch (profiles/k_z_c64_pwl128.md), scaled to the launch
+    traffic = None
+    if ZTRAFFIC_PER_RHS is not None and wl["pwl"] and n == 128:
+        traffic = ZTRAFFIC_PER_RHS * units + green
+    return {"kernel": "k_z<float,12> (z FFT + Green block multiply + iFFT)", "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "traffic": traffic, "alg_bytes_per_launch": alg, "launch_ms": round(ms_z, 4),
+            "units_per_launch": units, "peak_source": peak_kind}
+
+
+ZTRAFFIC_PER_RHS = None
+
+
+def run_ours(args, wl):
+    import torch
+    import torch.distributed as dist
+    from marie_gb300 import _lib
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as ge
+    if rank == 0:
+        ge.build()
+    if ws > 1:
+        dist.barrier()
+    ge.build()
+    op, body, b, t_asm = build_problem(wl, rank, torch)
+    nrhs = wl["nrhs"]
+    kw = dict(restart=50, tol=wl["tol"], maxit=200, mode="mixed", inner_tol=1e-5)
+    # warm-up (also the solve whose statistics are reported)
+    rep = None
+    for _ in range(args.warmup):
+        x, rep = op.gmres(b, **kw)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    launches0 = _lib.launch_count()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            x, rep = op.gmres(b, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = _lib.launch_count() - launches0
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = nrhs * args.steps * ws / (ms_max * 1e-3)
+
+    # end to end through the public API: pinned host b -> device, solve, x -> host
+    b_host = b.cpu().pin_memory()
+    x_host = torch.empty_like(b_host).pin_memory()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e2.record(stream)
+    nE = max(1, min(args.steps, 2))
+    for _ in range(nE):
+        bd = b_host.to("cuda", non_blocking=True)
+        xd, _r = op.gmres(bd, **kw)
+        x_host.copy_(xd, non_blocking=True)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3) / nE
+    e2e = {"value": round(nrhs * ws / (ms_e2e * 1e-3), 4), "unit": "solves/s",
+           "h2d_bytes_per_step": int(b_host.numel() * 16), "d2h_bytes_per_step": int(x_host.numel() * 16)}
+
+    # roofline of the dominant kernel (z pass, complex64) with CUDA events
+    peak, peak_kind = measured_peaks()
+    tiles = op.tiles()
+    xs = b[: op.Nb * min(nrhs, tiles["chunk"])].to(torch.complex64)
+    passes = op.profile(xs, reps=5)
+    roof = roofline_z(op, wl, tiles, passes[2], peak, peak_kind)
+    n, C, s = wl["n"], 12 if wl["pwl"] else 3, 8
+    U = 60 if wl["pwl"] else 6
+    units = xs.numel() // op.Nb
+    bmv = 26 * n ** 3 * C * s * units + U * (n + 1) ** 3 * s
+    roof["matvec"] = {"ms": round(passes[5], 4), "rhs": units, "alg_bytes": bmv,
+                      "achieved_GBs": round(bmv / (passes[5] * 1e-3) / 1e9, 1),
+                      "pass_ms": [round(v, 4) for v in passes[:5]]}
+
+    # FP64 GPU drop-in on one right-hand side (the plain complex128 method)
+    fp64 = None
+    if not args.skip_fp64:
+        b1 = b[: op.Nb].clone()
+        torch.cuda.synchronize()
+        t0 = time.time()
+        x64, rep64 = op.gmres(b1, restart=50, tol=wl["tol"], maxit=200, mode="fp64")
+        torch.cuda.synchronize()
+        dt = time.time() - t0
+        x32 = x[: op.Nb]
+        ferr = float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64))
+        fp64 = {"solves_per_s": round(1.0 / dt, 5), "iters": int(rep64.iters[0]),
+                "true_resid": float(rep64.true_resid[0]), "field_err_mixed_vs_fp64": ferr}
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else FP64_ITERS_CFG3), budget_s=args.cpu_budget)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32 accumulation) + FP64 refinement",
+            "data": "synthetic (seeded phantom, GPU-assembled Green's tensor, loop incident fields)",
+            "config": {"workload": wl["desc"], "grid": [wl["n"]] * 3, "basis": "PWL" if wl["pwl"] else "PWC",
+                       "n_body_voxels": int(body.idxS.size), "unknowns_per_rhs": int(op.Nb),
+                       "rhs_per_gpu": nrhs, "restart": 50, "tol": wl["tol"],
+                       "l2": "inputs larger than L2 (Krylov basis and FFT work arrays are tens of GB)",
+                       "parallelism": f"replicas x{ws} (independent RHS batches, no collective)"},
+            "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk.summary(), "roofline": roof, "cpu_baseline": cpu,
+            "solve": {"iters_per_rhs_mean": float(np.mean(rep.iters)), "matvecs_c64": int(rep.matvecs_c64),
+                      "matvecs_c128": int(rep.matvecs_c128), "true_resid_max": float(np.max(rep.true_resid)),
+                      "converged": int(np.sum(rep.status == 0))},
+            "fp64_gpu": fp64, "assembly_s": round(t_asm, 2),
+        }
+        print(json.dumps(line), flush=True)
+    op.close()
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(wl, iters, budget_s=30.0, steps=1, warmup=0):
+    """Time the CPU oracle (FP64 numpy/scipy restatement of mvp_vie + one
+    classical Gram-Schmidt Arnoldi step) on the full-size workload, all host
+    cores, and convert to solves/s with `iters` GMRES iterations per solve."""
+    from oracle import cpu_bench
+    r = cpu_bench.time_iteration(wl["n"], wl["pwl"], steps=steps, warmup=warmup, budget_s=budget_s)
+    sec_iter = r["sec_per_iter"]
+    return {"value": round(1.0 / (sec_iter * iters), 6), "unit": "solves/s", "cores": r["cores"], "kind": "port",
+            "sample": (f"{r['iters_timed']} GMRES iteration(s) (one FP64 mvp_vie with pre-expanded Green blocks + "
+                       f"one CGS Arnoldi step at k={r['k']}) on the full {wl['n']}^3 grid, "
+                       f"{r['sec_per_iter']:.2f} s each, x {iters} iterations/solve"),
+            "sec_per_iter": round(sec_iter, 3)}
+
+
+def run_reference(args, wl):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    cpu = cpu_baseline(wl, iters=FP64_ITERS_CFG3, budget_s=1e9, steps=args.steps, warmup=args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "solves/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": wl["desc"], "grid": [wl["n"]] * 3, "rhs_per_gpu": wl["nrhs"],
+                       "note": "MATLAB reference cannot run here; its FP64 algorithm is timed as the numpy/scipy "
+                               "port on the host cores"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg3", choices=sorted(WORKLOADS))
+    ap.add_argument("--nrhs", type=int, default=None)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    args = ap.parse_args()
+    wl = dict(WORKLOADS[args.workload])
+    if args.nrhs:
+        wl["nrhs"] = args.nrhs
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -152,6 +152,16 @@ marie_status marie_incident_loops(marie_vie* h, const double* origin, const doub
 marie_status marie_incident_plane_wave(marie_vie* h, const double* origin, void* out_dev, void* stream);
 
 /* Diagnostics. */
+/* Average device time [ms] of each matvec pass over `reps` repetitions of
+ * one mvp_vie application of nrhs right-hand sides (x/y: device, precision
+ * prec), timed with CUDA events on `stream`:
+ * ms[0] x-forward, ms[1] y-forward, ms[2] z (FFT, Green multiply, iFFT),
+ * ms[3] y-inverse, ms[4] x-inverse + epilogue.  ms[5] = whole application. */
+marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,
+                               double* ms, void* stream);
+/* Workspace right-hand sides per matvec chunk and the tile sizes in use:
+ * out[0] = chunk, out[1] = TY, out[2] = TXY, out[3] = TX. */
+marie_status marie_vie_tiles(marie_vie* h, int32_t prec, int32_t* out);
 const char* marie_last_error(void);
 const char* marie_version(void);
 /* Number of kernel launches issued by this library since load. */

@@ -229,8 +229,21 @@ static void set_smem_attr(const void* fn) {
 }
 
 template <typename T>
+static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
+                                     int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream,
+                                     cudaEvent_t* ev);
+
+template <typename T>
 marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
                            int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream) {
+  return launch_matvec_ev<T>(h, mode, op, in, in_rs, out, out_rs, nrhs, active, stream, nullptr);
+}
+
+// ev (optional): 6 events recorded around the 5 passes of the first chunk.
+template <typename T>
+static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
+                                     int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream,
+                                     cudaEvent_t* ev) {
   PrecState<T>& ps = prec_state<T>(h);
   if (!ps.built) {
     set_error("precision not built for this handle");
@@ -293,17 +306,24 @@ marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, in
     dim3 gx((n2 + a.TY - 1) / a.TY, n3, nr * C);
     dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nr * C);
     dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nr);
+    const bool rec = ev && r0 == 0;
+    if (rec) cudaEventRecord(ev[0], stream);
     k_fwd_x<T><<<gx, 256, smx, stream>>>(a);
     MARIE_LAUNCH_CHECK();
+    if (rec) cudaEventRecord(ev[1], stream);
     k_fwd_y<T><<<gy, 256, smy, stream>>>(a);
     MARIE_LAUNCH_CHECK();
+    if (rec) cudaEventRecord(ev[2], stream);
     if (C == 12) k_z<T, 12><<<gz, 256, smz, stream>>>(a, bt);
     else k_z<T, 3><<<gz, 256, smz, stream>>>(a, bt);
     MARIE_LAUNCH_CHECK();
+    if (rec) cudaEventRecord(ev[3], stream);
     k_inv_y<T><<<gy, 256, smy, stream>>>(a);
     MARIE_LAUNCH_CHECK();
+    if (rec) cudaEventRecord(ev[4], stream);
     k_inv_x<T><<<gx, 256, smx, stream>>>(a);
     MARIE_LAUNCH_CHECK();
+    if (rec) cudaEventRecord(ev[5], stream);
   }
   return MARIE_OK;
 }
@@ -491,6 +511,50 @@ marie_status marie_vie_apply_K(marie_vie* h, int32_t prec, const void* x, void* 
 }
 marie_status marie_vie_apply_K_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
   return apply_common(h, prec, x, y, nrhs, stream, MV_GRID, OP_K_ADJ);
+}
+
+marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,
+                               double* ms, void* stream) {
+  if (!h || !x || !y || !ms || nrhs < 1 || reps < 1) { set_error("marie_vie_profile: invalid argument"); return MARIE_ERR_BAD_ARG; }
+  if (prec != MARIE_C128 && prec != MARIE_C64) { set_error("prec must be MARIE_C128 or MARIE_C64"); return MARIE_ERR_BAD_ARG; }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev[6], t0, t1;
+  for (int i = 0; i < 6; ++i) cudaEventCreate(&ev[i]);
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  marie_status st = MARIE_OK;
+  for (int r = 0; r < reps && st == MARIE_OK; ++r) {
+    cudaEventRecord(t0, s);
+    if (prec == MARIE_C128)
+      st = launch_matvec_ev<double>(h, MV_VIE, OP_N, (const cplx<double>*)x, h->Nb, (cplx<double>*)y, h->Nb, nrhs,
+                                    nullptr, s, ev);
+    else
+      st = launch_matvec_ev<float>(h, MV_VIE, OP_N, (const cplx<float>*)x, h->Nb, (cplx<float>*)y, h->Nb, nrhs,
+                                   nullptr, s, ev);
+    cudaEventRecord(t1, s);
+    if (cudaEventSynchronize(t1) != cudaSuccess) { set_error("profile: device error"); st = MARIE_ERR_CUDA; break; }
+    for (int i = 0; i < 5; ++i) {
+      float v = 0;
+      cudaEventElapsedTime(&v, ev[i], ev[i + 1]);
+      acc[i] += v;
+    }
+    float w = 0;
+    cudaEventElapsedTime(&w, t0, t1);
+    acc[5] += w;
+  }
+  for (int i = 0; i < 6; ++i) ms[i] = acc[i] / reps;
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  return st;
+}
+
+marie_status marie_vie_tiles(marie_vie* h, int32_t prec, int32_t* out) {
+  if (!h || !out) { set_error("marie_vie_tiles: invalid argument"); return MARIE_ERR_BAD_ARG; }
+  if (prec == MARIE_C128) { out[0] = h->p64.ws_rhs; out[1] = h->p64.TY; out[2] = h->p64.TXY; out[3] = h->p64.TX; }
+  else { out[0] = h->p32.ws_rhs; out[1] = h->p32.TY; out[2] = h->p32.TXY; out[3] = h->p32.TX; }
+  return MARIE_OK;
 }
 
 const char* marie_last_error(void) { return t_err.c_str(); }

@@ -104,6 +104,67 @@ static unsigned grid_for(int64_t n) {
   return (unsigned)std::max<int64_t>(1, b);
 }
 
+// The octant storage needs the circulant parity of every block: a block that
+// is odd along an axis (mirror sign -1) must vanish on that axis' zero-offset
+// plane, otherwise G_hat(2n-k) != -G_hat(k).  Operators assembled by
+// assembly_N/K satisfy it to rounding (symmetric Gauss rules); reject others.
+static const double kParityTol = 1e-9;
+
+static marie_status check_parity_dense(const double* A, int n1, int n2, int n3, const int8_t s[3], int id) {
+  const int64_t nD = (int64_t)n1 * n2 * n3;
+  double mx = 0, bad = 0;
+  for (int64_t g = 0; g < nD; ++g) {
+    const double v = std::hypot(A[2 * g], A[2 * g + 1]);
+    mx = std::max(mx, v);
+    const int x = (int)(g % n1), y = (int)((g / n1) % n2), z = (int)(g / ((int64_t)n1 * n2));
+    if ((s[0] < 0 && x == 0) || (s[1] < 0 && y == 0) || (s[2] < 0 && z == 0)) bad = std::max(bad, v);
+  }
+  if (bad > kParityTol * mx) {
+    set_error("operator block %d violates the circulant parity (odd block nonzero on its zero-offset plane, "
+              "relative %.3e)", id, mx > 0 ? bad / mx : bad);
+    return MARIE_ERR_BAD_ARG;
+  }
+  return MARIE_OK;
+}
+
+// Tucker block: the zero-offset sample of factor column a along axis d is
+// u0[a] = (1/2n) sum_k U_d[a + r k] (inverse FFT at index 0).  Weighted by the
+// norm of the core slice it multiplies (the HOSVD singular value), it bounds
+// the block's value on the zero-offset plane relative to the block.
+static marie_status check_parity_tucker(const marie_tucker_block& t, int n1, int n2, int n3, const int8_t s[3],
+                                        int id) {
+  const int r[3] = {t.r1, t.r2, t.r3};
+  const int n[3] = {n1, n2, n3};
+  const double* U[3] = {t.U1, t.U2, t.U3};
+  for (int d = 0; d < 3; ++d) {
+    if (s[d] > 0) continue;
+    std::vector<double> sl(r[d], 0.0);
+    for (int c = 0; c < t.r3; ++c)
+      for (int b = 0; b < t.r2; ++b)
+        for (int a = 0; a < t.r1; ++a) {
+          const int64_t g = a + (int64_t)t.r1 * (b + (int64_t)t.r2 * c);
+          const double v2 = t.G[2 * g] * t.G[2 * g] + t.G[2 * g + 1] * t.G[2 * g + 1];
+          sl[d == 0 ? a : (d == 1 ? b : c)] += v2;
+        }
+    double smax = 0, worst = 0;
+    for (int a = 0; a < r[d]; ++a) smax = std::max(smax, std::sqrt(sl[a]));
+    for (int a = 0; a < r[d]; ++a) {
+      double sx = 0, sy = 0;
+      for (int k = 0; k < 2 * n[d]; ++k) {
+        sx += U[d][2 * (a + (int64_t)r[d] * k)];
+        sy += U[d][2 * (a + (int64_t)r[d] * k) + 1];
+      }
+      worst = std::max(worst, std::hypot(sx, sy) / (2.0 * n[d]) * std::sqrt(sl[a]));
+    }
+    if (worst > kParityTol * std::max(smax, 1e-300)) {
+      set_error("Tucker block %d violates the circulant parity along axis %d (odd block nonzero on its "
+                "zero-offset plane, relative %.3e)", id, d + 1, worst / smax);
+      return MARIE_ERR_BAD_ARG;
+    }
+  }
+  return MARIE_OK;
+}
+
 // Build all blocks of one operator (N or K) into the handle's spectra.
 static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const double* dense, int ncomp,
                              cplx<double>* dst64, cplx<float>* dst32) {
@@ -161,6 +222,8 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
         // dense I_V is (n1,n2,n3,pwx,ncomp) column-major: block (j,k) at (j + pwx*k)*nD
         const int j = id / ncomp, k = id % ncomp;
         const double* src = dense + 2 * ((int64_t)(j + pwx * k) * nD);
+        const int8_t sg[3] = {bt.s1[id], bt.s2[id], bt.s3[id]};
+        if ((st = check_parity_dense(src, n1, n2, n3, sg, id)) != MARIE_OK) break;
         if (cudaMemcpy(a, src, nD * sizeof(zd), cudaMemcpyHostToDevice) != cudaSuccess) {
           set_error("upload of dense I_V failed");
           st = MARIE_ERR_CUDA;
@@ -187,6 +250,8 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
           st = MARIE_ERR_BAD_ARG;
           break;
         }
+        const int8_t sg[3] = {bt.s1[id], bt.s2[id], bt.s3[id]};
+        if ((st = check_parity_tucker(t, n1, n2, n3, sg, id)) != MARIE_OK) break;
         mr1 = std::max(mr1, t.r1); mr2 = std::max(mr2, t.r2); mr3 = std::max(mr3, t.r3);
         mg = std::max<int64_t>(mg, (int64_t)t.r1 * t.r2 * t.r3);
         mp1 = std::max<int64_t>(mp1, (int64_t)t.r1 * t.r2 * nkz);

@@ -157,6 +157,22 @@ class VieOperator:
     def apply_K_adj(self, x, out=None):
         return self._apply(self._lib.marie_vie_apply_K_adj, x, self.C * self.nD, out)
 
+    def profile(self, x, reps=5):
+        """Per-pass device times [ms] of mvp_vie on x (CUDA events on the
+        current stream): x-fwd, y-fwd, z, y-inv, x-inv, whole application."""
+        import torch
+        prec = C128 if x.dtype == torch.complex128 else C64
+        y = torch.empty_like(x)
+        ms = np.zeros(6)
+        check(self._lib.marie_vie_profile(self._h, prec, ct.c_void_p(x.data_ptr()), ct.c_void_p(y.data_ptr()),
+                                          x.numel() // self.Nb, int(reps), _dptr(ms), self._stream()))
+        return ms
+
+    def tiles(self, prec=C64):
+        out = np.zeros(4, np.int32)
+        check(self._lib.marie_vie_tiles(self._h, prec, out.ctypes.data_as(_lib.c_int32_p)))
+        return dict(chunk=int(out[0]), TY=int(out[1]), TXY=int(out[2]), TX=int(out[3]))
+
     # -- solve ----------------------------------------------------------------
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-5,
               max_refine=10, resvec_cap=4096, raise_on_fail=False):

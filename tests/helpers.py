@@ -27,7 +27,20 @@ def synthetic_IV(n, pwl, kernel, seed):
     x, y, z = np.meshgrid(np.arange(n1), np.arange(n2), np.arange(n3), indexing="ij")
     decay = 1.0 / (1.0 + x ** 2 + y ** 2 + z ** 2)
     A = rng.normal(size=(n1, n2, n3, pwx, nc)) + 1j * rng.normal(size=(n1, n2, n3, pwx, nc))
-    return A * decay[..., None, None]
+    A = A * decay[..., None, None]
+    # circulant parity of the physical kernel: a block that is odd along an
+    # axis vanishes on that axis' zero-offset plane
+    g1, g2, g3 = O.G_N_SIGNS[nc]
+    for j in range(pwx):
+        for k in range(nc):
+            b = (O.BT_SIGNS[0][j], O.BT_SIGNS[1][j], O.BT_SIGNS[2][j]) if pwl else (1, 1, 1)
+            if g1[k] * b[0] < 0:
+                A[0, :, :, j, k] = 0
+            if g2[k] * b[1] < 0:
+                A[:, 0, :, j, k] = 0
+            if g3[k] * b[2] < 0:
+                A[:, :, 0, j, k] = 0
+    return A
 
 
 class Problem:

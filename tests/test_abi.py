@@ -93,6 +93,15 @@ def test_null_handle_calls(lib):
     assert lib.marie_vie_destroy(None) == 0
 
 
+def test_mex_gateway_compiles_against_stub():
+    """The MEX gateway (MATLAB caller of the C ABI) compiles against a
+    declaration-only mex.h; MATLAB itself is not available to run it."""
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                        "-I", str(ROOT / "tests" / "mex_stub"), "-I", str(ROOT / "include"),
+                        str(ROOT / "marie-tools_gb300" / "mex" / "marie_mex.c")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_header_compiles_as_c(tmp_path):
     src = tmp_path / "t.c"
     src.write_text('#include "marie_gb300.h"\nint main(void){marie_vie_desc d; (void)d; return 0;}\n')

@@ -108,3 +108,41 @@ def test_rerun_bit_identical():
     b = op.apply(x).cpu().numpy()
     assert np.array_equal(a, b)
     op.close()
+
+
+@pytest.mark.gpu
+def test_rejects_operator_without_circulant_parity():
+    from marie_gb300 import VieOperator
+    from marie_gb300._lib import MarieError
+    P = _problem((6, 5, 4), True)
+    rng = np.random.default_rng(0)
+    bad = rng.normal(size=P.IV_N.shape) + 1j * rng.normal(size=P.IV_N.shape)
+    with pytest.raises(MarieError, match="parity"):
+        VieOperator(P.n, P.res, P.freq, P.dims["idx_solution"], P.Mr, bad, pwl=True, precisions=1)
+    Tbad = O.assembly_fft_circ_tucker(bad, 1e-14)
+    with pytest.raises(MarieError, match="parity"):
+        VieOperator(P.n, P.res, P.freq, P.dims["idx_solution"], P.Mr, Tbad, pwl=True, precisions=1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["pwc_5", "pwl_4"])
+def test_physical_operator_parity(name):
+    """Assembled (physical) Green's tensors from the committed fixtures."""
+    from pathlib import Path
+    from marie_gb300 import VieOperator
+    g = Path(__file__).resolve().parent / "golden"
+    iv = np.load(g / f"iv_{name}.npz")
+    mv = np.load(g / f"mvp_{name}.npz")
+    n = tuple(int(v) for v in iv["n"])
+    pwl = bool(iv["pwl"])
+    emc = O.em_constants(float(iv["freq"]))
+    ep = O.em_assembly(mv["er"], mv["se"], emc["ce"])
+    dims = O.geo_dims(*n, mv["idxS"], pwl, float(iv["res"]))
+    T = O.assembly_fft_circ_tucker(iv["N"] if pwl else iv["N"][:, :, :, 0, :], float(mv["tucker_tol"]))
+    op = VieOperator(n, float(iv["res"]), float(iv["freq"]), dims["idx_solution"], ep["Mr"], T, pwl=pwl)
+    for prec, dt in (("c128", torch.complex128), ("c64", torch.complex64)):
+        y = op.apply(torch.from_numpy(mv["Jb"]).to("cuda", dt)).cpu().numpy()
+        assert rel_err(y, mv["AJ"]) <= TOL[prec]
+        yN = op.apply_N(torch.from_numpy(flat_F(mv["J"])).to("cuda", dt)).cpu().numpy()
+        assert rel_err(unflat_F(yN, n, 12 if pwl else 3), mv["NJ"]) <= TOL[prec]
+    op.close()
