@@ -174,7 +174,7 @@ def run_ours(args, wl):
     ge.build()
     op, body, b, t_asm = build_problem(wl, rank, torch)
     nrhs = wl["nrhs"]
-    kw = dict(restart=50, tol=wl["tol"], maxit=200, mode="mixed", inner_tol=1e-5)
+    kw = dict(restart=50, tol=wl["tol"], maxit=200, mode="mixed", inner_tol=1e-7)
     # warm-up (also the solve whose statistics are reported)
     rep = None
     for _ in range(args.warmup):

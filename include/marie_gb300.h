@@ -111,7 +111,8 @@ typedef struct {
   double tol;             /* relative residual target */
   int32_t mode;           /* marie_solve_mode */
   int32_t x0_present;     /* 1: x holds the initial guess; 0: start from zero */
-  double inner_tol;       /* MIXED: inner c64 GMRES relative tolerance (e.g. 1e-4) */
+  double inner_tol;       /* MIXED: floor of the inner c64 GMRES relative tolerance (0 = 1e-7);
+                             each inner solve asks for max(inner_tol, 0.3*tol/current residual) */
   int32_t max_refine;     /* MIXED: max refinement steps */
 } marie_gmres_opts;
 
@@ -159,8 +160,9 @@ marie_status marie_incident_plane_wave(marie_vie* h, const double* origin, void*
  * ms[3] y-inverse, ms[4] x-inverse + epilogue.  ms[5] = whole application. */
 marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,
                                double* ms, void* stream);
-/* Workspace right-hand sides per matvec chunk and the tile sizes in use:
- * out[0] = chunk, out[1] = TY, out[2] = TXY, out[3] = TX. */
+/* Workspace right-hand sides per matvec chunk and the z-pass tile width:
+ * out[0] = chunk, out[1] = tile width (pencils x interleaved right-hand
+ * sides), out[2..3] reserved (0). */
 marie_status marie_vie_tiles(marie_vie* h, int32_t prec, int32_t* out);
 const char* marie_last_error(void);
 const char* marie_version(void);

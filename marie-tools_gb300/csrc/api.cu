@@ -187,15 +187,34 @@ static void make_tables(marie_vie* h) {
   }
 }
 
+// Z-pass tile width W = TX*R (contiguous elements per (component, z) row):
+// the largest power of two whose shared-memory tile fits ~100 KB (two CTAs per
+// SM).  The bundle size R is at most W.
 template <typename T>
 static void choose_tiles(marie_vie* h, PrecState<T>& ps) {
-  const int n1 = h->n1, n2 = h->n2, n3 = h->n3, C = h->C;
+  const int n3 = h->n3, C = h->C;
   const int sz = (int)sizeof(cplx<T>);
-  ps.TY = std::max(1, std::min(n2, (sizeof(T) == 4 ? 2048 : 1024) / std::max(1, n1)));
-  ps.TXY = std::max(1, std::min(2 * n1, sizeof(T) == 4 ? 16 : 8));
-  int TX = 32;
-  while (TX > 1 && (size_t)n3 * (2 * C * TX + 1) * sz > 100 * 1024) TX /= 2;
-  ps.TX = std::max(1, std::min(TX, 2 * n1));
+  int W = 16;
+  while (W > 1 && (size_t)n3 * (2 * C * W + 1) * sz > 100 * 1024) W /= 2;
+  ps.TX = W;      // Wz
+  ps.TY = 0;
+  ps.TXY = 0;
+}
+
+struct CallTiles {
+  int R, TY, TXY, TX;
+};
+
+template <typename T>
+static CallTiles call_tiles(const marie_vie* h, const PrecState<T>& ps, int nr) {
+  CallTiles t;
+  const int Wz = ps.TX;
+  t.R = std::max(1, std::min(Wz, nr));
+  const int wxy = sizeof(T) == 4 ? 16 : 8;   // sequences per row tile of the x/y passes
+  t.TY = std::max(1, std::min(h->n2, wxy / t.R));
+  t.TXY = std::max(1, std::min(2 * h->n1, wxy / t.R));
+  t.TX = std::max(1, std::min(2 * h->n1, Wz / t.R));
+  return t;
 }
 
 template <typename T>
@@ -217,6 +236,8 @@ template <typename T>
 static marie_status alloc_workspace(marie_vie* h, PrecState<T>& ps) {
   const int64_t per = (int64_t)h->C * h->n3 * h->n2 * 2 * h->n1;  // T1 per rhs
   int ws = std::max(1, std::min(h->max_rhs, env_int("MARIE_WS_RHS", 16)));
+  const int Wz = ps.TX;
+  if (ws > Wz) ws = (ws + Wz - 1) / Wz * Wz;   // whole bundles
   ps.ws_rhs = ws;
   MARIE_TRY(dev_alloc(h, (void**)&ps.T1, (size_t)ws * per * sizeof(cplx<T>)));
   MARIE_TRY(dev_alloc(h, (void**)&ps.S, (size_t)ws * per * 2 * sizeof(cplx<T>)));
@@ -232,6 +253,34 @@ template <typename T>
 static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
                                      int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream,
                                      cudaEvent_t* ev);
+
+template <typename T, bool PWL, int OP>
+static void launch_z(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute((const void*)k_z<T, PWL, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  });
+  k_z<T, PWL, OP><<<g, 256, smem, s>>>(a);
+}
+
+template <typename T>
+static void dispatch_z(bool pwl, int op, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+  if (pwl) {
+    switch (op) {
+      case OP_N: launch_z<T, true, 0>(a, g, smem, s); break;
+      case OP_N_ADJ: launch_z<T, true, 1>(a, g, smem, s); break;
+      case OP_K: launch_z<T, true, 2>(a, g, smem, s); break;
+      default: launch_z<T, true, 3>(a, g, smem, s); break;
+    }
+  } else {
+    switch (op) {
+      case OP_N: launch_z<T, false, 0>(a, g, smem, s); break;
+      case OP_N_ADJ: launch_z<T, false, 1>(a, g, smem, s); break;
+      case OP_K: launch_z<T, false, 2>(a, g, smem, s); break;
+      default: launch_z<T, false, 3>(a, g, smem, s); break;
+    }
+  }
+}
 
 template <typename T>
 marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
@@ -258,14 +307,10 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   std::call_once(once, [] {
     set_smem_attr<T>((const void*)k_fwd_x<float>);
     set_smem_attr<T>((const void*)k_fwd_y<float>);
-    set_smem_attr<T>((const void*)k_z<float, 3>);
-    set_smem_attr<T>((const void*)k_z<float, 12>);
     set_smem_attr<T>((const void*)k_inv_y<float>);
     set_smem_attr<T>((const void*)k_inv_x<float>);
     set_smem_attr<T>((const void*)k_fwd_x<double>);
     set_smem_attr<T>((const void*)k_fwd_y<double>);
-    set_smem_attr<T>((const void*)k_z<double, 3>);
-    set_smem_attr<T>((const void*)k_z<double, 12>);
     set_smem_attr<T>((const void*)k_inv_y<double>);
     set_smem_attr<T>((const void*)k_inv_x<double>);
   });
@@ -286,26 +331,28 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   a.T1 = ps.T1;
   a.S = ps.S;
   a.G = isK ? ps.GK : ps.GN;
-  a.TY = ps.TY;
-  a.TXY = ps.TXY;
-  a.TX = ps.TX;
   a.in_rs = in_rs;
   a.out_rs = out_rs;
-  const BlockTab& bt = h->tab[op];
   const int n1 = h->n1, n2 = h->n2, n3 = h->n3, C = h->C;
   const size_t sz = sizeof(cplx<T>);
-  const size_t smx = (size_t)(n1 + 2 * a.TY * n1) * sz;
-  const size_t smy = (size_t)(n2 + 2 * n2 * a.TXY) * sz;
-  const size_t smz = (size_t)(n3 + (size_t)n3 * (2 * C * a.TX + 1)) * sz;
   for (int r0 = 0; r0 < nrhs; r0 += ps.ws_rhs) {
     const int nr = std::min(ps.ws_rhs, nrhs - r0);
+    const CallTiles ct = call_tiles(h, ps, nr);
+    const int nb = (nr + ct.R - 1) / ct.R;
+    a.R = ct.R;
+    a.TY = ct.TY;
+    a.TXY = ct.TXY;
+    a.TX = ct.TX;
     a.nrhs = nr;
     a.in = in + (int64_t)r0 * in_rs;
     a.out = out + (int64_t)r0 * out_rs;
     a.active = active ? active + r0 : nullptr;
-    dim3 gx((n2 + a.TY - 1) / a.TY, n3, nr * C);
-    dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nr * C);
-    dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nr);
+    const size_t smx = (size_t)(n1 + (size_t)n1 * (2 * a.TY * a.R + 1)) * sz;
+    const size_t smy = (size_t)(n2 + (size_t)n2 * (2 * a.TXY * a.R + 1)) * sz;
+    const size_t smz = (size_t)(n3 + (size_t)n3 * (2 * C * a.TX * a.R + 1)) * sz;
+    dim3 gx((n2 + a.TY - 1) / a.TY, n3, nb * C);
+    dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nb * C);
+    dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nb);
     const bool rec = ev && r0 == 0;
     if (rec) cudaEventRecord(ev[0], stream);
     k_fwd_x<T><<<gx, 256, smx, stream>>>(a);
@@ -314,8 +361,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
     k_fwd_y<T><<<gy, 256, smy, stream>>>(a);
     MARIE_LAUNCH_CHECK();
     if (rec) cudaEventRecord(ev[2], stream);
-    if (C == 12) k_z<T, 12><<<gz, 256, smz, stream>>>(a, bt);
-    else k_z<T, 3><<<gz, 256, smz, stream>>>(a, bt);
+    dispatch_z<T>(h->pwl != 0, op, a, gz, smz, stream);
     MARIE_LAUNCH_CHECK();
     if (rec) cudaEventRecord(ev[3], stream);
     k_inv_y<T><<<gy, 256, smy, stream>>>(a);
@@ -552,8 +598,8 @@ marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* 
 
 marie_status marie_vie_tiles(marie_vie* h, int32_t prec, int32_t* out) {
   if (!h || !out) { set_error("marie_vie_tiles: invalid argument"); return MARIE_ERR_BAD_ARG; }
-  if (prec == MARIE_C128) { out[0] = h->p64.ws_rhs; out[1] = h->p64.TY; out[2] = h->p64.TXY; out[3] = h->p64.TX; }
-  else { out[0] = h->p32.ws_rhs; out[1] = h->p32.TY; out[2] = h->p32.TXY; out[3] = h->p32.TX; }
+  if (prec == MARIE_C128) { out[0] = h->p64.ws_rhs; out[1] = h->p64.TX; out[2] = 0; out[3] = 0; }
+  else { out[0] = h->p32.ws_rhs; out[1] = h->p32.TX; out[2] = 0; out[3] = 0; }
   return MARIE_OK;
 }
 

@@ -40,6 +40,23 @@ __device__ __forceinline__ void fma_c(cplx<T>& acc, cplx<T> a, cplx<T> b) {
   acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
 }
 
+// Read-only (non-coherent cache) load of a complex value.
+__device__ __forceinline__ cplx<float> ldg_c(const cplx<float>* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+__device__ __forceinline__ cplx<double> ldg_c(const cplx<double>* p) {
+  const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+  return {v.x, v.y};
+}
+
+// acc -= a * b
+template <typename T>
+__device__ __forceinline__ void fms_c(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+  acc.x = fma(-a.x, b.x, fma(a.y, b.y, acc.x));
+  acc.y = fma(-a.x, b.y, fma(-a.y, b.x, acc.y));
+}
+
 // Multiply by -i (forward transform sign) or +i (inverse).
 template <typename T, bool INV>
 __device__ __forceinline__ cplx<T> mul_mi(cplx<T> a) {

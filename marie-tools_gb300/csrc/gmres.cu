@@ -93,16 +93,29 @@ __global__ void k_dots(const cplx<T>* V, int64_t ld, int64_t Nb, int k, int mp1,
   }
 }
 
-// H[r][j + (m+1) k] = sum_chunk part, j in [0,k]
-__global__ void k_reduce_dots(const zd* part, int nch, int k, int mp1, int m, const unsigned char* act, zd* H) {
-  const int r = blockIdx.x;
-  if (!act[r]) return;
-  for (int j = threadIdx.x; j <= k; j += blockDim.x) {
-    const zd* p = part + ((int64_t)r * mp1 + j) * nch;
-    double sx = 0, sy = 0;
-    for (int c = 0; c < nch; ++c) { sx += p[c].x; sy += p[c].y; }
-    H[(int64_t)r * mp1 * m + j + (int64_t)mp1 * k] = zd{sx, sy};
+// Deterministic warp sum of per-CTA partials: lane l adds chunks l, l+32, ...
+// in order, then a fixed butterfly tree.
+__device__ __forceinline__ zd warp_sum_partials(const zd* p, int nch) {
+  const int lane = threadIdx.x & 31;
+  double sx = 0, sy = 0;
+  for (int c = lane; c < nch; c += 32) { sx += p[c].x; sy += p[c].y; }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
   }
+  return zd{sx, sy};
+}
+
+// H[r][j + (m+1) k] = sum_chunk part, j in [0,k]; one warp per (rhs, j).
+// grid (ceil((k+1)/8), nrhs), 256 threads.
+__global__ void k_reduce_dots(const zd* part, int nch, int k, int mp1, int m, const unsigned char* act, zd* H) {
+  const int r = blockIdx.y;
+  if (!act[r]) return;
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (j > k) return;
+  const zd s = warp_sum_partials(part + ((int64_t)r * mp1 + j) * nch, nch);
+  if ((threadIdx.x & 31) == 0) H[(int64_t)r * mp1 * m + j + (int64_t)mp1 * k] = s;
 }
 
 // w -= sum_j V_j h_j ; npart[r*nch + chunk] = ||w_chunk||^2
@@ -177,13 +190,17 @@ __global__ void k_norm2(const cplx<T>* v, int64_t rs, int64_t Nb, const unsigned
   if (threadIdx.x == 0) npart[(int64_t)r * nch + blockIdx.x] = (double)s.x;
 }
 
-// out[r] = sqrt(sum_chunk npart)
+// out[r] = sqrt(sum_chunk npart); one warp per rhs, grid (ceil(nrhs/8)), 256 threads.
 __global__ void k_reduce_norm(const double* npart, int nch, int nrhs, const unsigned char* act, double* out) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (r >= nrhs || (act && !act[r])) return;
+  const int lane = threadIdx.x & 31;
+  const double* p = npart + (int64_t)r * nch;
   double s = 0;
-  for (int c = 0; c < nch; ++c) s += npart[(int64_t)r * nch + c];
-  out[r] = sqrt(s);
+  for (int c = lane; c < nch; c += 32) s += p[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[r] = sqrt(s);
 }
 
 // v_r *= 1/s_r  (zero when s_r == 0)
@@ -444,7 +461,7 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
   // beta = ||r0||
   k_norm2<T><<<cg, kVT, 0, s>>>(V, vrs, Nb, d_mask, st.npart, nch);
   MARIE_LAUNCH_CHECK();
-  k_reduce_norm<<<sb, 128, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
+  k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
   MARIE_LAUNCH_CHECK();
   std::vector<double> beta(nrhs, 0.0);
   MARIE_CUDA_TRY(cudaMemcpyAsync(beta.data(), st.beta, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -477,11 +494,11 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
       ++*matvecs;
       k_dots<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, st.incyc, st.part, nch);
       MARIE_LAUNCH_CHECK();
-      k_reduce_dots<<<nrhs, 64, 0, s>>>(st.part, nch, k, mp1, m, st.incyc, st.H);
+      k_reduce_dots<<<dim3((k + 8) / 8, nrhs), 256, 0, s>>>(st.part, nch, k, mp1, m, st.incyc, st.H);
       MARIE_LAUNCH_CHECK();
       k_update<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, m, st.incyc, st.H, st.npart, nch);
       MARIE_LAUNCH_CHECK();
-      k_reduce_norm<<<sb, 128, 0, s>>>(st.npart, nch, nrhs, st.incyc, st.hnorm);
+      k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, st.incyc, st.hnorm);
       MARIE_LAUNCH_CHECK();
       // scale with the mask before the Givens step clears finished rhs
       k_scale<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V + (int64_t)(k + 1) * ld, vrs, Nb, st.incyc, st.hnorm);
@@ -512,7 +529,7 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     MARIE_LAUNCH_CHECK();
     k_norm2<T><<<cg, kVT, 0, s>>>(V, vrs, Nb, d_mask, st.npart, nch);
     MARIE_LAUNCH_CHECK();
-    k_reduce_norm<<<sb, 128, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
+    k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
     MARIE_LAUNCH_CHECK();
     MARIE_CUDA_TRY(cudaStreamSynchronize(s));
     nstart = 0;
@@ -549,7 +566,7 @@ static marie_status true_residual(marie_vie* h, int nrhs, const zd* b, const zd*
   MARIE_LAUNCH_CHECK();
   k_norm2<double><<<dim3(nch, nrhs), kVT, 0, s>>>((const cplx<double>*)r, Nb, Nb, d_mask, npart, nch);
   MARIE_LAUNCH_CHECK();
-  k_reduce_norm<<<(nrhs + 127) / 128, 128, 0, s>>>(npart, nch, nrhs, d_mask, nr);
+  k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(npart, nch, nrhs, d_mask, nr);
   MARIE_LAUNCH_CHECK();
   std::vector<double> v(nrhs);
   MARIE_CUDA_TRY(cudaMemcpyAsync(v.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -568,7 +585,7 @@ static marie_status norms(marie_vie* h, int nrhs, const zd* v, std::vector<doubl
   MARIE_TRY(sc.get(&nr, nrhs));
   k_norm2<double><<<dim3(nch, nrhs), kVT, 0, s>>>((const cplx<double>*)v, Nb, Nb, nullptr, npart, nch);
   MARIE_LAUNCH_CHECK();
-  k_reduce_norm<<<(nrhs + 127) / 128, 128, 0, s>>>(npart, nch, nrhs, nullptr, nr);
+  k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(npart, nch, nrhs, nullptr, nr);
   MARIE_LAUNCH_CHECK();
   out.resize(nrhs);
   MARIE_CUDA_TRY(cudaMemcpyAsync(out.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -654,7 +671,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
       MARIE_CUDA_TRY(cudaMemcpyAsync(r64, b, sizeof(zd) * Nb * nrhs, cudaMemcpyDeviceToDevice, s));
       for (int r = 0; r < nrhs; ++r) rel[r] = bnorm[r] > 0 ? 1.0 : 0.0;
     }
-    const double floor_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+    const double floor_tol = o->inner_tol > 0 ? o->inner_tol : 1e-7;
     const int max_refine = o->max_refine > 0 ? o->max_refine : 10;
     for (int it = 0; it < max_refine; ++it) {
       std::vector<unsigned char> todo(nrhs, 0);

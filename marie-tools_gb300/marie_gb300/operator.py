@@ -171,10 +171,10 @@ class VieOperator:
     def tiles(self, prec=C64):
         out = np.zeros(4, np.int32)
         check(self._lib.marie_vie_tiles(self._h, prec, out.ctypes.data_as(_lib.c_int32_p)))
-        return dict(chunk=int(out[0]), TY=int(out[1]), TXY=int(out[2]), TX=int(out[3]))
+        return dict(chunk=int(out[0]), width=int(out[1]))
 
     # -- solve ----------------------------------------------------------------
-    def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-5,
+    def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
               max_refine=10, resvec_cap=4096, raise_on_fail=False):
         """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA."""
         import torch
