@@ -100,6 +100,23 @@ marie_status marie_vie_apply_N_adj(marie_vie* h, int32_t prec, const void* x, vo
 marie_status marie_vie_apply_K(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
 marie_status marie_vie_apply_K_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
 
+/* Allocation-free y = mvp_N(x) for ONE complex64 right-hand side, without a
+ * handle.  No counterpart in the reference: it is for callers that must not
+ * allocate device memory (an allocator-free region of a host framework, a
+ * real-time loop, a process that reserved all device memory up front) and so
+ * cannot call marie_vie_create.  The caller passes device pointers: the N
+ * octant spectrum green_octant (complex64, layout [blk][n2+1][n1+1][n3+1],
+ * blk = j*6+k for block T(j+1,k+1), scaled by 1/(8 n1 n2 n3)), x and y (grids,
+ * n1*n2*n3*C, column-major).  The FFT work arrays live in a fixed 64 MiB
+ * file-scope device array, so 6*n1*n2*n3*C*8 bytes must not exceed 64 MiB
+ * (larger grids return MARIE_ERR_BAD_ARG).  That array is held by every GPU
+ * that loads the library until exit and is shared by all calls: calls that
+ * overlap on the GPU race.  The first call on a device looks up the array's
+ * device address; make it before any stream capture.  Never calls cudaMalloc
+ * or cudaFree. */
+marie_status marie_vie_apply_N_noalloc(int32_t n1, int32_t n2, int32_t n3, int32_t basis,
+                                       const void* green_octant, const void* x, void* y, void* stream);
+
 typedef enum {
   MARIE_SOLVE_FP64 = 0,   /* complex128 GMRES, faithful to is_gmres_vie.m */
   MARIE_SOLVE_MIXED = 1   /* complex64 GMRES inside an FP64 iterative-refinement loop */
