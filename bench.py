@@ -302,6 +302,33 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def run_matvec_only(args, wl):
+    """Operator applications only (no solver state on the device): the small,
+    bounded command used for ncu captures of the matvec kernels."""
+    import torch
+    import __graft_entry__ as ge
+    from marie_gb300 import VieOperator, assemble_green, phantoms
+    ge.build()
+    torch.cuda.set_device(0)
+    n, res, freq, pwl = wl["n"], wl["res"], wl["freq"], wl["pwl"]
+    body = phantoms.ellipsoid_phantom(n, res, seed=0) if wl["phantom"] != "sphere" else phantoms.sphere(n, res)
+    ivN = assemble_green(body.n, res, freq, pwl, "N")
+    prec = 2 if args.prec == "c64" else 1
+    op = VieOperator(body.n, res, freq, body.idx_solution(pwl), body.Mr(freq), ivN, pwl=pwl, precisions=prec,
+                     max_rhs=wl["nrhs"])
+    del ivN
+    dt = torch.complex64 if args.prec == "c64" else torch.complex128
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn(wl["nrhs"] * op.Nb, dtype=dt, device="cuda", generator=g)
+    for _ in range(args.matvec_only):
+        op.apply(x)
+    torch.cuda.synchronize()
+    ms = op.profile(x, reps=3)
+    print(json.dumps({"matvec_only": wl["desc"], "prec": args.prec, "nrhs": wl["nrhs"],
+                      "pass_ms": [round(v, 4) for v in ms[:5]], "matvec_ms": round(ms[5], 4)}), flush=True)
+    op.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -313,10 +340,16 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=30.0)
+    ap.add_argument("--matvec-only", type=int, default=0,
+                    help="profiling aid: build the workload, apply mvp_vie this many times, print per-pass times")
+    ap.add_argument("--prec", default="c64", choices=["c64", "c128"], help="precision of --matvec-only")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
     if args.nrhs:
         wl["nrhs"] = args.nrhs
+    if args.matvec_only:
+        run_matvec_only(args, wl)
+        return
     if args.impl == "reference":
         run_reference(args, wl)
     else:
