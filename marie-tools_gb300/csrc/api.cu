@@ -205,17 +205,27 @@ struct CallTiles {
   int R, TY, TXY, TX;
 };
 
+static int pow2floor(int v) {
+  int p = 1;
+  while (p * 2 <= v) p *= 2;
+  return p;
+}
+
+// Bundle size R (a power of two, <= the z tile width) and the tiles of one
+// chunk of nr right-hand sides.  fast: four-step passes (wider x/y tiles).
 template <typename T>
-static CallTiles call_tiles(const marie_vie* h, const PrecState<T>& ps, int nr) {
+static CallTiles call_tiles(const marie_vie* h, const PrecState<T>& ps, int nr, bool fast) {
   CallTiles t;
   const int Wz = ps.TX;
-  t.R = std::max(1, std::min(Wz, nr));
-  const int wxy = sizeof(T) == 4 ? 16 : 8;   // sequences per row tile of the x/y passes
+  t.R = pow2floor(std::max(1, std::min(Wz, nr)));
+  const int wxy = (sizeof(T) == 4 ? 16 : 8) * (fast ? 2 : 1);   // row-tile width of the x/y passes
   t.TY = std::max(1, std::min(h->n2, wxy / t.R));
   t.TXY = std::max(1, std::min(2 * h->n1, wxy / t.R));
   t.TX = std::max(1, std::min(2 * h->n1, Wz / t.R));
   return t;
 }
+
+static bool four_step_edge(int n) { return n % 16 == 0 && n / 16 >= 1 && n / 16 <= 8; }
 
 template <typename T>
 static void fill_axis(AxisTab<T>& dst, const AxisDev<T>& src) {
@@ -239,8 +249,9 @@ static marie_status alloc_workspace(marie_vie* h, PrecState<T>& ps) {
   const int Wz = ps.TX;
   if (ws > Wz) ws = (ws + Wz - 1) / Wz * Wz;   // whole bundles
   ps.ws_rhs = ws;
-  MARIE_TRY(dev_alloc(h, (void**)&ps.T1, (size_t)ws * per * sizeof(cplx<T>)));
-  MARIE_TRY(dev_alloc(h, (void**)&ps.S, (size_t)ws * per * 2 * sizeof(cplx<T>)));
+  const int64_t alloc = (int64_t)(ws + Wz - 1) / Wz * Wz;   // any chunk of <= ws rhs fits whole bundles
+  MARIE_TRY(dev_alloc(h, (void**)&ps.T1, (size_t)alloc * per * sizeof(cplx<T>)));
+  MARIE_TRY(dev_alloc(h, (void**)&ps.S, (size_t)alloc * per * 2 * sizeof(cplx<T>)));
   return MARIE_OK;
 }
 
@@ -337,9 +348,13 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   const size_t sz = sizeof(cplx<T>);
   for (int r0 = 0; r0 < nrhs; r0 += ps.ws_rhs) {
     const int nr = std::min(ps.ws_rhs, nrhs - r0);
-    const CallTiles ct = call_tiles(h, ps, nr);
+    const bool fast = four_step_edge(n1) && four_step_edge(n2) && four_step_edge(n3) &&
+                      (op == OP_N || op == OP_N_ADJ) && !env_int("MARIE_GENERIC_FFT", 0);
+    const CallTiles ct = call_tiles(h, ps, nr, fast);
     const int nb = (nr + ct.R - 1) / ct.R;
     a.R = ct.R;
+    a.lgR = 0;
+    while ((1 << a.lgR) < a.R) ++a.lgR;
     a.TY = ct.TY;
     a.TXY = ct.TXY;
     a.TX = ct.TX;
@@ -347,6 +362,10 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
     a.in = in + (int64_t)r0 * in_rs;
     a.out = out + (int64_t)r0 * out_rs;
     a.active = active ? active + r0 : nullptr;
+    if (fast) {
+      MARIE_TRY(launch_fast_chunk<T>(h, op, a, nb, stream, (ev && r0 == 0) ? ev : nullptr));
+      continue;
+    }
     const size_t smx = (size_t)(n1 + (size_t)n1 * (2 * a.TY * a.R + 1)) * sz;
     const size_t smy = (size_t)(n2 + (size_t)n2 * (2 * a.TXY * a.R + 1)) * sz;
     const size_t smz = (size_t)(n3 + (size_t)n3 * (2 * C * a.TX * a.R + 1)) * sz;

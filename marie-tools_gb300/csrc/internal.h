@@ -105,6 +105,11 @@ marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, in
 template <typename T>
 PrecState<T>& prec_state(marie_vie* h);
 
+// Four-step passes (grid edges 16*NB, NB <= 8) for one chunk of nb bundles;
+// tiles and bundle size are set in `a` by the caller.
+template <typename T>
+marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaStream_t stream, cudaEvent_t* ev);
+
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
 
 }  // namespace marie

@@ -64,6 +64,7 @@ template <typename T>
 struct MvArgs {
   int n1, n2, n3, C;
   int R;                      // right-hand sides per bundle (interleaved innermost)
+  int lgR;                    // log2(R) (R is a power of two)
   int nrhs;                   // right-hand sides in this launch (<= nbundle * R)
   int64_t Ns;                 // body voxels
   int mode;

@@ -146,3 +146,35 @@ def test_physical_operator_parity(name):
         yN = op.apply_N(torch.from_numpy(flat_F(mv["J"])).to("cuda", dt)).cpu().numpy()
         assert rel_err(unflat_F(yN, n, 12 if pwl else 3), mv["NJ"]) <= TOL[prec]
     op.close()
+
+
+FAST_SIZES = [(16, 16, 16), (32, 16, 48), (48, 32, 16)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
+@pytest.mark.parametrize("n", FAST_SIZES, ids=lambda n: "x".join(map(str, n)))
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_four_step_path(n, pwl, prec, monkeypatch):
+    """Grids with edges 16*NB take the four-step register FFT path for N and
+    N^H; it must match the oracle and the generic shared-memory path."""
+    P = _problem(n, pwl)
+    op = P.gpu_operator(max_rhs=4)
+    J = P.random_grid(seed=8, nrhs=3)
+    x = torch.from_numpy(np.concatenate([flat_F(J[r]) for r in range(3)])).to("cuda", _dt(prec))
+    for name, adj, fn in (("N", False, op.apply_N), ("N", True, op.apply_N_adj)):
+        y = fn(x).cpu().numpy().astype(np.complex128)
+        monkeypatch.setenv("MARIE_GENERIC_FFT", "1")
+        yg = fn(x).cpu().numpy().astype(np.complex128)
+        monkeypatch.delenv("MARIE_GENERIC_FFT")
+        for r in range(3):
+            ref = O.mvp_op_tucker(J[r], P.TN, name, adj, cache={})
+            sl = slice(r * J[r].size, (r + 1) * J[r].size)
+            assert rel_err(unflat_F(y[sl], n, P.C), ref) <= TOL[prec]
+            assert rel_err(y[sl], yg[sl]) <= TOL[prec]
+    X = P.random_body_vec(seed=6, nrhs=5)
+    xb = torch.from_numpy(X.reshape(-1)).to("cuda", _dt(prec))
+    yb = op.apply(xb).cpu().numpy().reshape(5, -1).astype(np.complex128)
+    for r in range(5):
+        assert rel_err(yb[r], O.mvp_vie(X[r], P.Mr, P.Mc, P.dims, P.TN, cache={})) <= TOL[prec]
+    op.close()
