@@ -78,7 +78,7 @@ marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaS
   const size_t sz = sizeof(cplx<T>);
   const size_t smx = (size_t)(n1 + (size_t)2 * a.TY * a.R * (n1 + 1)) * sz;
   const size_t smy = (size_t)(n2 + (size_t)2 * a.TXY * a.R * (n2 + 1)) * sz;
-  const size_t smz = (size_t)(n3 + (size_t)2 * C * a.TX * a.R * (n3 + 1)) * sz;
+  const size_t smz = kz4_smem<T>(n3, C, a.TX * a.R);
   dim3 gx((n2 + a.TY - 1) / a.TY, n3, nb * C);
   dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nb * C);
   dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nb);

@@ -190,11 +190,13 @@ __global__ void k_fwd_y(MvArgs<T> a) {
 // One entry of the z-pass Green multiply, every index a compile-time constant:
 // load block blk's value when the entry starts a new block (entries are sorted
 // by block), then y[p] += sgn * G_blk * x[q] for both points of the work item.
-template <typename T, bool PWL, int OP, int K>
+// TWO: the second point has its own octant value (at gp1) and no z-mirror
+// sign; otherwise it is the z-mirror of the first (same value, sign s3).
+template <typename T, bool PWL, int OP, int K, bool TWO>
 struct ZStep {
   static __device__ __forceinline__ void run(cplx<T>* y0, cplx<T>* y1, const cplx<T>* x0, const cplx<T>* x1,
                                              cplx<T>& g0v, cplx<T>& g1v, const cplx<T>* gp0, const cplx<T>* gp1,
-                                             int64_t gblk, bool mx, bool my, bool mirror) {
+                                             int64_t gblk, bool mx, bool my) {
     using Tab = OpTab<PWL, OP>;
     constexpr int blk = Tab::L.e[K].blk;
     constexpr int p = Tab::L.e[K].p, q = Tab::L.e[K].q, sg = Tab::L.e[K].sgn;
@@ -202,15 +204,16 @@ struct ZStep {
     if constexpr (first) {
       constexpr bool neg1 = Tab::L.s1[blk] < 0, neg2 = Tab::L.s2[blk] < 0, neg3 = Tab::L.s3[blk] < 0;
       cplx<T> gA = ldg_c(gp0 + blk * gblk);
-      cplx<T> gB = ldg_c(gp1 + blk * gblk);
-      if constexpr ((OP & 1) != 0) {
-        gA = conjg(gA);
-        gB = conjg(gB);
-      }
+      if constexpr ((OP & 1) != 0) gA = conjg(gA);
       const bool f = (neg1 && mx) != (neg2 && my);    // sign flip from x/y mirrors
       g0v = f ? cplx<T>{-gA.x, -gA.y} : gA;
-      const bool f1 = f != (neg3 && mirror);
-      g1v = f1 ? cplx<T>{-gB.x, -gB.y} : gB;
+      if constexpr (TWO) {
+        cplx<T> gB = ldg_c(gp1 + blk * gblk);
+        if constexpr ((OP & 1) != 0) gB = conjg(gB);
+        g1v = f ? cplx<T>{-gB.x, -gB.y} : gB;
+      } else {
+        g1v = neg3 ? cplx<T>{-g0v.x, -g0v.y} : g0v;
+      }
     }
     if constexpr (sg > 0) {
       fma_c(y0[p], g0v, x0[q]);
@@ -222,12 +225,34 @@ struct ZStep {
   }
 };
 
-template <typename T, bool PWL, int OP, int... Ks>
+template <typename T, bool PWL, int OP, bool TWO, int... Ks>
 __device__ __forceinline__ void zmul(std::integer_sequence<int, Ks...>, cplx<T>* y0, cplx<T>* y1, const cplx<T>* x0,
                                      const cplx<T>* x1, const cplx<T>* gp0, const cplx<T>* gp1, int64_t gblk, bool mx,
-                                     bool my, bool mirror) {
+                                     bool my) {
   cplx<T> g0v = {0, 0}, g1v = {0, 0};
-  (ZStep<T, PWL, OP, Ks>::run(y0, y1, x0, x1, g0v, g1v, gp0, gp1, gblk, mx, my, mirror), ...);
+  (ZStep<T, PWL, OP, Ks, TWO>::run(y0, y1, x0, x1, g0v, g1v, gp0, gp1, gblk, mx, my), ...);
+}
+
+// Green multiply of one work item: y = G x at two frequencies.
+template <typename T, bool PWL, int OP, bool TWO>
+__device__ __forceinline__ void zitem(cplx<T>* buf, int o0, int o1, int qstride, const cplx<T>* gp0,
+                                      const cplx<T>* gp1, int64_t gblk, bool mx, bool my) {
+  constexpr int C = PWL ? 12 : 3;
+  cplx<T> x0[C], x1[C], y0[C], y1[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) {
+    x0[q] = buf[o0 + q * qstride];
+    x1[q] = buf[o1 + q * qstride];
+    y0[q] = cplx<T>{0, 0};
+    y1[q] = cplx<T>{0, 0};
+  }
+  zmul<T, PWL, OP, TWO>(std::make_integer_sequence<int, OpTab<PWL, OP>::NE>{}, y0, y1, x0, x1, gp0, gp1, gblk, mx,
+                        my);
+#pragma unroll
+  for (int p = 0; p < C; ++p) {
+    buf[o0 + p * qstride] = y0[p];
+    buf[o1 + p * qstride] = y1[p];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -292,23 +317,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_z(MvArgs<T> a) 
     const int kz1 = u == 0 ? n3 : 2 * n3 - u;
     const int r0 = kz0 >> 1, g0 = kz0 & 1;
     const int r1 = (kz1 >> 1) % n3, g1 = kz1 & 1;
-    cplx<T> x0[C], x1[C], y0[C], y1[C];
-#pragma unroll
-    for (int q = 0; q < C; ++q) {
-      x0[q] = buf[r0 * es + (g0 * C + q) * W + e];
-      x1[q] = buf[r1 * es + (g1 * C + q) * W + e];
-      y0[q] = cplx<T>{0, 0};
-      y1[q] = cplx<T>{0, 0};
-    }
+    const int o0 = r0 * es + g0 * C * W + e, o1 = r1 * es + g1 * C * W + e;
     const cplx<T>* gp0 = a.G + ((int64_t)kyo * (n1 + 1) + kxo) * nko + u;
-    const cplx<T>* gp1 = u == 0 ? gp0 + n3 : gp0;
     // the second point is a z-mirror (sign s3) unless u == 0 (frequency n3)
-    zmul<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, y0, y1, x0, x1, gp0, gp1, gblk, mx, my, u != 0);
-#pragma unroll
-    for (int p = 0; p < C; ++p) {
-      buf[r0 * es + (g0 * C + p) * W + e] = y0[p];
-      buf[r1 * es + (g1 * C + p) * W + e] = y1[p];
-    }
+    if (u != 0) zitem<T, PWL, OP, false>(buf, o0, o1, W, gp0, gp0, gblk, mx, my);
+    else zitem<T, PWL, OP, true>(buf, o0, o1, W, gp0, gp0 + n3, gblk, mx, my);
   }
   __syncthreads();
   fft_dif<T, true>(buf, nseq, es, 1, a.az.plan, tw, true);

@@ -94,7 +94,7 @@ __device__ __forceinline__ void dftn(cplx<T>* v) {
 // buf: sequence s = (yy*R + r)*2 + alpha, stride S = 16*NB + 1, [k1][b]
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256) k4_fwd_x(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, 3) k4_fwd_x(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) k4_fwd_x(MvArgs<T> a) {
 // Pass XI (inverse x + crop + epilogue), n1 = 16*NB.
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256) k4_inv_x(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, 3) k4_inv_x(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(256) k4_inv_x(MvArgs<T> a) {
 // buf: sequence s = beta*W + e, stride S, [k1][b]
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256) k4_fwd_y(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, 3) k4_fwd_y(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(256) k4_fwd_y(MvArgs<T> a) {
 // Pass YI (inverse y + crop), n2 = 16*NB.
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256) k4_inv_y(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, 3) k4_inv_y(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -338,134 +338,6 @@ __global__ void __launch_bounds__(256) k4_inv_y(MvArgs<T> a) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// Pass Z (fused), n3 = 16*NB.  grid (ceil(2n1/TX), 2n2, nbundle)
-// buf: sequence s = (gamma*C + c)*W + e, stride S, [k1][b] (then [k1][k2])
-// ---------------------------------------------------------------------------
-template <typename T, int NB, bool PWL, int OP>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k4_z(MvArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int N = 16 * NB, S = N + 1;
-  constexpr int C = PWL ? 12 : 3;
-  constexpr int NE = OpTab<PWL, OP>::NE;
-  const int bu = blockIdx.z;
-  if (!bundle_active(a, bu)) return;
-  const int kyp = blockIdx.y, k0 = blockIdx.x * a.TX;
-  const int n1 = a.n1, n2 = a.n2, m1 = 2 * n1, R = a.R;
-  const int W = a.TX * R, wl = min(a.TX, m1 - k0) * R;
-  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* buf = tw + N;
-  load_tw(tw, a.az.tw, N);
-  __syncthreads();
-  const int64_t row = (int64_t)m1 * R;
-  const int64_t cstride = (int64_t)2 * n2 * N * row;
-  cplx<T>* base = a.S + (int64_t)bu * C * cstride + (int64_t)kyp * N * row + (int64_t)k0 * R;
-  // forward step 1: task (c, b, e), e fastest
-  for (int t = threadIdx.x; t < C * NB * W; t += blockDim.x) {
-    const int e = t % W, q2 = t / W;
-    const int b = q2 % NB, c = q2 / NB;
-    cplx<T> v[16], u[16];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const cplx<T> val = e < wl ? base[c * cstride + (int64_t)(NB * q + b) * row + e] : cplx<T>{0, 0};
-      v[q] = val;
-      u[q] = val;
-    }
-    dftn<T, false, 16>(u);
-    cplx<T>* d0 = buf + (c * W + e) * S + b;
-#pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) d0[k1 * NB] = u[k1] * tw[b * k1];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) u[q] = v[q] * a.az.tw2[NB * q + b];
-    dftn<T, false, 16>(u);
-    cplx<T>* d1 = buf + ((C + c) * W + e) * S + b;
-#pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) d1[k1 * NB] = u[k1] * tw[b * k1];
-  }
-  __syncthreads();
-  // forward step 2 (in place): task (seq, k1), seq fastest
-  for (int t = threadIdx.x; t < 2 * C * W * 16; t += blockDim.x) {
-    const int s = t % (2 * C * W), k1 = t / (2 * C * W);
-    cplx<T>* p = buf + s * S + k1 * NB;
-    cplx<T> w[NB];
-#pragma unroll
-    for (int b = 0; b < NB; ++b) w[b] = p[b];
-    dftn<T, false, NB>(w);
-#pragma unroll
-    for (int k2 = 0; k2 < NB; ++k2) p[k2] = w[k2];
-  }
-  __syncthreads();
-  // Green block multiply: item (u, e), points kz0 = u (0 -> 0) and kz1 = 2N - u
-  // (0 -> N); frequency kz = 2k + gamma sits at [gamma][k & 15][k >> 4].
-  const int beta = kyp / n2, ky = 2 * (kyp - beta * n2) + beta;
-  const bool my = ky > n2;
-  const int kyo = my ? 2 * n2 - ky : ky;
-  const int nko = N + 1;
-  const int64_t gblk = (int64_t)(n2 + 1) * (n1 + 1) * nko;
-  for (int i = threadIdx.x; i < N * W; i += blockDim.x) {
-    const int e = i % W, u = i / W;
-    const int t = e / R;
-    const int kxp = k0 + t;
-    if (kxp >= m1) continue;
-    const int alpha = kxp / n1;
-    const int kx = 2 * (kxp - alpha * n1) + alpha;
-    const bool mx = kx > n1;
-    const int kxo = mx ? 2 * n1 - kx : kx;
-    const int kz0 = u, kz1 = u == 0 ? N : 2 * N - u;
-    const int o0 = (((kz0 & 1) * C) * W + e) * S + ((kz0 >> 1) & 15) * NB + ((kz0 >> 1) >> 4);
-    const int o1 = (((kz1 & 1) * C) * W + e) * S + (((kz1 >> 1) % N) & 15) * NB + (((kz1 >> 1) % N) >> 4);
-    cplx<T> x0[C], x1[C], y0[C], y1[C];
-#pragma unroll
-    for (int q = 0; q < C; ++q) {
-      x0[q] = buf[o0 + q * W * S];
-      x1[q] = buf[o1 + q * W * S];
-      y0[q] = cplx<T>{0, 0};
-      y1[q] = cplx<T>{0, 0};
-    }
-    const cplx<T>* gp0 = a.G + ((int64_t)kyo * (n1 + 1) + kxo) * nko + u;
-    const cplx<T>* gp1 = u == 0 ? gp0 + N : gp0;
-    zmul<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, y0, y1, x0, x1, gp0, gp1, gblk, mx, my, u != 0);
-#pragma unroll
-    for (int p = 0; p < C; ++p) {
-      buf[o0 + p * W * S] = y0[p];
-      buf[o1 + p * W * S] = y1[p];
-    }
-  }
-  __syncthreads();
-  // inverse step A (in place): task (seq, k1)
-  for (int t = threadIdx.x; t < 2 * C * W * 16; t += blockDim.x) {
-    const int s = t % (2 * C * W), k1 = t / (2 * C * W);
-    cplx<T>* p = buf + s * S + k1 * NB;
-    cplx<T> w[NB];
-#pragma unroll
-    for (int k2 = 0; k2 < NB; ++k2) w[k2] = p[k2];
-    dftn<T, true, NB>(w);
-#pragma unroll
-    for (int b = 0; b < NB; ++b) p[b] = mulc(w[b], tw[b * k1]);
-  }
-  __syncthreads();
-  // inverse step B: task (c, b, e): both halves, combine, store
-  for (int t = threadIdx.x; t < C * NB * W; t += blockDim.x) {
-    const int e = t % W, q2 = t / W;
-    const int b = q2 % NB, c = q2 / NB;
-    const cplx<T>* s0 = buf + (c * W + e) * S + b;
-    const cplx<T>* s1 = buf + ((C + c) * W + e) * S + b;
-    cplx<T> u0[16], u1[16];
-#pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) {
-      u0[k1] = s0[k1 * NB];
-      u1[k1] = s1[k1 * NB];
-    }
-    dftn<T, true, 16>(u0);
-    dftn<T, true, 16>(u1);
-    if (e < wl) {
-#pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int zz = NB * q + b;
-        base[c * cstride + (int64_t)zz * row + e] = u0[q] + mulc(u1[q], a.az.tw2[zz]);
-      }
-    }
-  }
-}
-
 }  // namespace marie
+
+#include "kz4.cuh"
