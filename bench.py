@@ -42,7 +42,7 @@ METRIC = "GMRES solves/s at 128^3 PWL, 1e-6 resid (mixed c64/FP64-refined, 64-RH
 # workload, measured by this library's complex128 solver (same algorithm as
 # is_gmres_vie.m); used to turn the reference arm's per-iteration time into
 # solves/s.  Updated from the 'fp64_iters_per_solve' field of our own arm.
-FP64_ITERS_CFG3 = 60.0
+FP64_ITERS_CFG3 = 13.0
 
 
 def _dist():
@@ -149,7 +149,9 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind):
     traffic = None
     if ZTRAFFIC_PER_RHS is not None and wl["pwl"] and n == 128:
         traffic = ZTRAFFIC_PER_RHS * units + green
-    return {"kernel": "k_z<float,12> (z FFT + Green block multiply + iFFT)", "bound": "hbm",
+    four_step = n % 16 == 0 and 16 <= n <= 128
+    name = (f"k4_z<float,{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
+    return {"kernel": name + " (z FFT + Green block multiply + inverse z FFT)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "traffic": traffic, "alg_bytes_per_launch": alg, "launch_ms": round(ms_z, 4),
             "units_per_launch": units, "peak_source": peak_kind}
