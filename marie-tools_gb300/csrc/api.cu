@@ -53,6 +53,19 @@ template <>
 PrecState<double>& prec_state<double>(marie_vie* h) { return h->p64; }
 template <>
 PrecState<float>& prec_state<float>(marie_vie* h) { return h->p32; }
+template <>
+PrecState<ff>& prec_state<ff>(marie_vie* h) { return h->pff; }
+
+// Host conversion of a table value to the device arithmetic type.
+template <typename T>
+static T prec_from(long double v) {
+  if constexpr (std::is_same<T, ff>::value) {
+    const float hi = (float)v;
+    return ff(hi, (float)(v - (long double)hi));
+  } else {
+    return (T)v;
+  }
+}
 
 // n = product of radices; 8s first, then 4, 2, then odd primes.
 static bool make_plan(int n, FftPlan* pl) {
@@ -103,8 +116,8 @@ static marie_status build_axis(marie_vie* h, int n, AxisDev<T>& ax) {
   for (int k = 0; k < n; ++k) {
     const long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)n;
     const long double b = a / 2.0L;
-    tw[k] = cplx<T>{(T)std::cos(a), (T)std::sin(a)};
-    tw2[k] = cplx<T>{(T)std::cos(b), (T)std::sin(b)};
+    tw[k] = cplx<T>{prec_from<T>(std::cos(a)), prec_from<T>(std::sin(a))};
+    tw2[k] = cplx<T>{prec_from<T>(std::cos(b)), prec_from<T>(std::sin(b))};
   }
   std::vector<int> kofp, pofk;
   digit_maps(ax.plan, kofp, pofk);
@@ -261,9 +274,9 @@ static void set_smem_attr(const void* fn) {
 }
 
 template <typename T>
-static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
-                                     int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream,
-                                     cudaEvent_t* ev);
+static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<typename IoOf<T>::type>* in,
+                                     int64_t in_rs, cplx<typename IoOf<T>::type>* out, int64_t out_rs, int nrhs,
+                                     const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev);
 
 template <typename T, bool PWL, int OP>
 static void launch_z(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
@@ -293,17 +306,24 @@ static void dispatch_z(bool pwl, int op, const MvArgs<T>& a, dim3 g, size_t smem
   }
 }
 
+// complex128 calls run on the float-float state when the handle was built
+// with it instead of native FP64 (precisions bit 4).
+static bool c128_is_ff(const marie_vie* h) { return !h->p64.built && h->pff.built; }
+
 template <typename T>
 marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
                            int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (c128_is_ff(h)) return launch_matvec_ev<ff>(h, mode, op, in, in_rs, out, out_rs, nrhs, active, stream, nullptr);
+  }
   return launch_matvec_ev<T>(h, mode, op, in, in_rs, out, out_rs, nrhs, active, stream, nullptr);
 }
 
 // ev (optional): 6 events recorded around the 5 passes of the first chunk.
 template <typename T>
-static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<T>* in, int64_t in_rs, cplx<T>* out,
-                                     int64_t out_rs, int nrhs, const unsigned char* active, cudaStream_t stream,
-                                     cudaEvent_t* ev) {
+static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<typename IoOf<T>::type>* in,
+                                     int64_t in_rs, cplx<typename IoOf<T>::type>* out, int64_t out_rs, int nrhs,
+                                     const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev) {
   PrecState<T>& ps = prec_state<T>(h);
   if (!ps.built) {
     set_error("precision not built for this handle");
@@ -338,7 +358,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   fill_axis(a.az, ps.az);
   a.vox2sol = h->vox2sol;
   a.chi = ps.chi;
-  for (int c = 0; c < h->C; ++c) a.invg[c] = (T)h->invg[c];
+  for (int c = 0; c < h->C; ++c) a.invg[c] = prec_from<T>(h->invg[c]);
   a.T1 = ps.T1;
   a.S = ps.S;
   a.G = isK ? ps.GK : ps.GN;
@@ -366,6 +386,11 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
       MARIE_TRY(launch_fast_chunk<T>(h, op, a, nb, stream, (ev && r0 == 0) ? ev : nullptr));
       continue;
     }
+    if constexpr (std::is_same<T, ff>::value) {
+      set_error("the float-float complex128 operator covers N and N^H on grids with edges 16*NB (NB <= 8); "
+                "build the handle with native complex128 (precisions bit 1) for this call");
+      return MARIE_ERR_NOT_SUPPORTED;
+    } else {
     const size_t smx = (size_t)(n1 + (size_t)n1 * (2 * a.TY * a.R + 1)) * sz;
     const size_t smy = (size_t)(n2 + (size_t)n2 * (2 * a.TXY * a.R + 1)) * sz;
     const size_t smz = (size_t)(n3 + (size_t)n3 * (2 * C * a.TX * a.R + 1)) * sz;
@@ -389,6 +414,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
     k_inv_x<T><<<gx, 256, smx, stream>>>(a);
     MARIE_LAUNCH_CHECK();
     if (rec) cudaEventRecord(ev[5], stream);
+    }
   }
   return MARIE_OK;
 }
@@ -414,7 +440,16 @@ static marie_status validate_desc(const marie_vie_desc* d, std::vector<int64_t>&
   if (!d->idx_solution || d->n_b <= 0) { set_error("idx_solution is empty"); return MARIE_ERR_BAD_ARG; }
   if (!d->Mr) { set_error("Mr is NULL"); return MARIE_ERR_BAD_ARG; }
   if (!d->tucker_N && !d->dense_N) { set_error("neither tucker_N nor dense_N given"); return MARIE_ERR_BAD_ARG; }
-  if (d->precisions < 1 || d->precisions > 3) { set_error("precisions must be 1, 2 or 3"); return MARIE_ERR_BAD_ARG; }
+  if (d->precisions < 1 || d->precisions > 7) { set_error("precisions must be a nonzero mask of bits 1, 2 and 4"); return MARIE_ERR_BAD_ARG; }
+  if ((d->precisions & 1) && (d->precisions & 4)) {
+    set_error("precisions bits 1 (native complex128) and 4 (float-float complex128) are exclusive");
+    return MARIE_ERR_BAD_ARG;
+  }
+  if ((d->precisions & 4) && !(four_step_edge(d->n1) && four_step_edge(d->n2) && four_step_edge(d->n3))) {
+    set_error("float-float complex128 (precisions bit 4) needs grid edges 16*NB with NB <= 8, got %d x %d x %d",
+              d->n1, d->n2, d->n3);
+    return MARIE_ERR_NOT_SUPPORTED;
+  }
   if (d->max_rhs < 1) { set_error("max_rhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
   const int C = d->basis == MARIE_PWL ? 12 : 3;
   if (d->n_b % C != 0) { set_error("n_b=%lld is not a multiple of %d components", (long long)d->n_b, C); return MARIE_ERR_BAD_ARG; }
@@ -504,9 +539,20 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
     chi[s] = cplx<double>{v.real(), v.imag()};
   }
   (void)e0;
-  for (int pr = 0; pr < 2; ++pr) {
+  for (int pr = 0; pr < 3; ++pr) {
     if (!(d->precisions & (1 << pr))) continue;
-    if (pr == 0) {
+    if (pr == 2) {
+      PrecState<ff>& ps = h->pff;
+      if ((st = build_axis(h, h->n1, ps.ax)) != MARIE_OK) return fail(st);
+      if ((st = build_axis(h, h->n2, ps.ay)) != MARIE_OK) return fail(st);
+      if ((st = build_axis(h, h->n3, ps.az)) != MARIE_OK) return fail(st);
+      std::vector<cplx<ff>> chiff(h->Ns);
+      for (int64_t s = 0; s < h->Ns; ++s) chiff[s] = cplx<ff>{prec_from<ff>(chi[s].x), prec_from<ff>(chi[s].y)};
+      if ((st = dev_alloc(h, (void**)&ps.chi, h->Ns * sizeof(cplx<ff>))) != MARIE_OK) return fail(st);
+      cudaMemcpy(ps.chi, chiff.data(), h->Ns * sizeof(cplx<ff>), cudaMemcpyHostToDevice);
+      choose_tiles(h, ps);
+      if ((st = alloc_workspace(h, ps)) != MARIE_OK) return fail(st);
+    } else if (pr == 0) {
       PrecState<double>& ps = h->p64;
       if ((st = build_axis(h, h->n1, ps.ax)) != MARIE_OK) return fail(st);
       if ((st = build_axis(h, h->n2, ps.ay)) != MARIE_OK) return fail(st);
@@ -531,6 +577,7 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   if ((st = build_spectra(h, d)) != MARIE_OK) return fail(st);
   if (h->precisions & 1) h->p64.built = true;
   if (h->precisions & 2) h->p32.built = true;
+  if (h->precisions & 4) h->pff.built = true;
   if (cudaDeviceSynchronize() != cudaSuccess) {
     set_error("device error during create: %s", cudaGetErrorString(cudaGetLastError()));
     return fail(MARIE_ERR_CUDA);
@@ -591,7 +638,10 @@ marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* 
   marie_status st = MARIE_OK;
   for (int r = 0; r < reps && st == MARIE_OK; ++r) {
     cudaEventRecord(t0, s);
-    if (prec == MARIE_C128)
+    if (prec == MARIE_C128 && c128_is_ff(h))
+      st = launch_matvec_ev<ff>(h, MV_VIE, OP_N, (const cplx<double>*)x, h->Nb, (cplx<double>*)y, h->Nb, nrhs,
+                                nullptr, s, ev);
+    else if (prec == MARIE_C128)
       st = launch_matvec_ev<double>(h, MV_VIE, OP_N, (const cplx<double>*)x, h->Nb, (cplx<double>*)y, h->Nb, nrhs,
                                     nullptr, s, ev);
     else
@@ -617,7 +667,8 @@ marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* 
 
 marie_status marie_vie_tiles(marie_vie* h, int32_t prec, int32_t* out) {
   if (!h || !out) { set_error("marie_vie_tiles: invalid argument"); return MARIE_ERR_BAD_ARG; }
-  if (prec == MARIE_C128) { out[0] = h->p64.ws_rhs; out[1] = h->p64.TX; out[2] = 0; out[3] = 0; }
+  if (prec == MARIE_C128 && c128_is_ff(h)) { out[0] = h->pff.ws_rhs; out[1] = h->pff.TX; out[2] = 1; out[3] = 0; }
+  else if (prec == MARIE_C128) { out[0] = h->p64.ws_rhs; out[1] = h->p64.TX; out[2] = 0; out[3] = 0; }
   else { out[0] = h->p32.ws_rhs; out[1] = h->p32.TX; out[2] = 0; out[3] = 0; }
   return MARIE_OK;
 }

@@ -1,62 +1,31 @@
-// Launch code of the four-step matvec passes (matvec4.cuh), instantiated per
-// precision in fast_f32.cu / fast_f64.cu.
+// Launch code of the four-step matvec passes (matvec4.cuh, kz4.cuh).
+//
+// The per-pass launchers (switch over NB = n/16) are declared here and
+// defined in fastpath_impl.cuh, so that one precision's kernels can be spread
+// over several translation units that compile in parallel (the float-float
+// kernels: x and y passes in two units, the z pass in one object per NB).
 #pragma once
 
-#include <mutex>
-
 #include "internal.h"
-#include "matvec4.cuh"
 
 namespace marie {
 
-template <typename KernelFn>
-static void smem_opt_in(KernelFn fn, std::once_flag& once) {
-  std::call_once(once, [fn] {
-    cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  });
+__host__ __device__ constexpr int kz4_stride(int N, int W) { return N + (W >= 16 ? 1 : 16 / W); }
+__host__ __device__ constexpr int kz4_halfpad(int W) { return W >= 16 ? 0 : 8 / W; }
+
+// Shared-memory bytes of k4_z: twiddles + both halves.
+template <typename T>
+__host__ inline size_t kz4_smem(int N, int C, int W) {
+  const size_t half = (size_t)C * W * kz4_stride(N, W);
+  return (N + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
 }
 
-template <typename T, int NB>
-static void launch_x(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag of, oi;
-  if (!inv) {
-    smem_opt_in(k4_fwd_x<T, NB>, of);
-    k4_fwd_x<T, NB><<<g, 256, smem, s>>>(a);
-  } else {
-    smem_opt_in(k4_inv_x<T, NB>, oi);
-    k4_inv_x<T, NB><<<g, 256, smem, s>>>(a);
-  }
-}
-
-template <typename T, int NB>
-static void launch_y(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag of, oi;
-  if (!inv) {
-    smem_opt_in(k4_fwd_y<T, NB>, of);
-    k4_fwd_y<T, NB><<<g, 256, smem, s>>>(a);
-  } else {
-    smem_opt_in(k4_inv_y<T, NB>, oi);
-    k4_inv_y<T, NB><<<g, 256, smem, s>>>(a);
-  }
-}
-
-template <typename T, int NB, bool PWL, int OP>
-static void launch_z4(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag o;
-  smem_opt_in(k4_z<T, NB, PWL, OP>, o);
-  k4_z<T, NB, PWL, OP><<<g, 256, smem, s>>>(a);
-}
-
-template <typename T, int NB>
-static void launch_z_nb(bool pwl, int op, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  if (pwl) {
-    if (op == OP_N) launch_z4<T, NB, true, 0>(a, g, smem, s);
-    else launch_z4<T, NB, true, 1>(a, g, smem, s);
-  } else {
-    if (op == OP_N) launch_z4<T, NB, false, 0>(a, g, smem, s);
-    else launch_z4<T, NB, false, 1>(a, g, smem, s);
-  }
-}
+template <typename T>
+void launch_x_nb(int nb, bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s);
+template <typename T>
+void launch_y_nb(int nb, bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s);
+template <typename T, bool PWL, int NB>
+void launch_z_one(int op, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s);
 
 #define MARIE_NB_SWITCH(nb, CALL) \
   switch (nb) {                   \
@@ -70,6 +39,13 @@ static void launch_z_nb(bool pwl, int op, const MvArgs<T>& a, dim3 g, size_t sme
     default: CALL(8); break;      \
   }
 
+template <typename T, bool PWL>
+void launch_z_nb(int nb, int op, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+#define Z_CALL(NB) launch_z_one<T, PWL, NB>(op, a, g, smem, s)
+  MARIE_NB_SWITCH(nb, Z_CALL);
+#undef Z_CALL
+}
+
 // The five passes of one chunk on the four-step path; ev (optional) as in
 // launch_matvec_ev.  Tiles in `a` are set by the caller.
 template <typename T>
@@ -82,31 +58,21 @@ marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaS
   dim3 gx((n2 + a.TY - 1) / a.TY, n3, nb * C);
   dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nb * C);
   dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nb);
-  const bool pwl = h->pwl != 0;
   if (ev) cudaEventRecord(ev[0], stream);
-#define X_FWD(NB) launch_x<T, NB>(false, a, gx, smx, stream)
-  MARIE_NB_SWITCH(n1 / 16, X_FWD);
-#undef X_FWD
+  launch_x_nb<T>(n1 / 16, false, a, gx, smx, stream);
   MARIE_LAUNCH_CHECK();
   if (ev) cudaEventRecord(ev[1], stream);
-#define Y_FWD(NB) launch_y<T, NB>(false, a, gy, smy, stream)
-  MARIE_NB_SWITCH(n2 / 16, Y_FWD);
-#undef Y_FWD
+  launch_y_nb<T>(n2 / 16, false, a, gy, smy, stream);
   MARIE_LAUNCH_CHECK();
   if (ev) cudaEventRecord(ev[2], stream);
-#define Z_ALL(NB) launch_z_nb<T, NB>(pwl, op, a, gz, smz, stream)
-  MARIE_NB_SWITCH(n3 / 16, Z_ALL);
-#undef Z_ALL
+  if (h->pwl) launch_z_nb<T, true>(n3 / 16, op, a, gz, smz, stream);
+  else launch_z_nb<T, false>(n3 / 16, op, a, gz, smz, stream);
   MARIE_LAUNCH_CHECK();
   if (ev) cudaEventRecord(ev[3], stream);
-#define Y_INV(NB) launch_y<T, NB>(true, a, gy, smy, stream)
-  MARIE_NB_SWITCH(n2 / 16, Y_INV);
-#undef Y_INV
+  launch_y_nb<T>(n2 / 16, true, a, gy, smy, stream);
   MARIE_LAUNCH_CHECK();
   if (ev) cudaEventRecord(ev[4], stream);
-#define X_INV(NB) launch_x<T, NB>(true, a, gx, smx, stream)
-  MARIE_NB_SWITCH(n1 / 16, X_INV);
-#undef X_INV
+  launch_x_nb<T>(n1 / 16, true, a, gx, smx, stream);
   MARIE_LAUNCH_CHECK();
   if (ev) cudaEventRecord(ev[5], stream);
   return MARIE_OK;

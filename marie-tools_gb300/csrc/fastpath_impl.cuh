@@ -1,0 +1,70 @@
+// Definitions of the four-step pass launchers declared in fastpath.cuh.
+#pragma once
+
+#include <mutex>
+
+#include "fastpath.cuh"
+#include "matvec4.cuh"
+
+namespace marie {
+
+template <typename KernelFn>
+static void smem_opt_in(KernelFn fn, std::once_flag& once) {
+  std::call_once(once, [fn] {
+    cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  });
+}
+
+template <typename T, int NB>
+static void launch_x(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+  static std::once_flag of, oi;
+  if (!inv) {
+    smem_opt_in(k4_fwd_x<T, NB>, of);
+    k4_fwd_x<T, NB><<<g, 256, smem, s>>>(a);
+  } else {
+    smem_opt_in(k4_inv_x<T, NB>, oi);
+    k4_inv_x<T, NB><<<g, 256, smem, s>>>(a);
+  }
+}
+
+template <typename T, int NB>
+static void launch_y(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+  static std::once_flag of, oi;
+  if (!inv) {
+    smem_opt_in(k4_fwd_y<T, NB>, of);
+    k4_fwd_y<T, NB><<<g, 256, smem, s>>>(a);
+  } else {
+    smem_opt_in(k4_inv_y<T, NB>, oi);
+    k4_inv_y<T, NB><<<g, 256, smem, s>>>(a);
+  }
+}
+
+template <typename T, int NB, bool PWL, int OP>
+static void launch_z4(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+  static std::once_flag o;
+  smem_opt_in(k4_z<T, NB, PWL, OP>, o);
+  k4_z<T, NB, PWL, OP><<<g, 256, smem, s>>>(a);
+}
+
+template <typename T>
+void launch_x_nb(int nb, bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+#define X_CALL(NB) launch_x<T, NB>(inv, a, g, smem, s)
+  MARIE_NB_SWITCH(nb, X_CALL);
+#undef X_CALL
+}
+
+template <typename T>
+void launch_y_nb(int nb, bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+#define Y_CALL(NB) launch_y<T, NB>(inv, a, g, smem, s)
+  MARIE_NB_SWITCH(nb, Y_CALL);
+#undef Y_CALL
+}
+
+// The four-step path serves N (op 0) and N^H (op 1).
+template <typename T, bool PWL, int NB>
+void launch_z_one(int op, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
+  if (op == OP_N) launch_z4<T, NB, PWL, 0>(a, g, smem, s);
+  else launch_z4<T, NB, PWL, 1>(a, g, smem, s);
+}
+
+}  // namespace marie

@@ -625,7 +625,10 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
   if (o->maxit < 0) { set_error("maxit must be >= 0"); return MARIE_ERR_BAD_ARG; }
   if (!(o->tol > 0)) { set_error("tol must be > 0"); return MARIE_ERR_BAD_ARG; }
   if (o->mode != MARIE_SOLVE_FP64 && o->mode != MARIE_SOLVE_MIXED) { set_error("unknown solve mode"); return MARIE_ERR_BAD_ARG; }
-  if (!h->p64.built) { set_error("GMRES needs the complex128 operator (precisions bit 1)"); return MARIE_ERR_BAD_ARG; }
+  if (!h->p64.built && !h->pff.built) {
+    set_error("GMRES needs a complex128 operator (precisions bit 1 or 4)");
+    return MARIE_ERR_BAD_ARG;
+  }
   if (o->mode == MARIE_SOLVE_MIXED && !h->p32.built) { set_error("mixed mode needs the complex64 operator (precisions bit 2)"); return MARIE_ERR_BAD_ARG; }
   cudaStream_t s = (cudaStream_t)stream;
   const zd* b = (const zd*)b_;

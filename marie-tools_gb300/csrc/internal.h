@@ -80,6 +80,7 @@ struct marie_vie {
   marie::BlockTab tab[4];            // N, N_adj, K, K_adj
   marie::PrecState<double> p64;
   marie::PrecState<float> p32;
+  marie::PrecState<marie::ff> pff;   // complex128 I/O, float-float arithmetic (precisions bit 4)
   std::vector<void*> allocs;
   // GMRES scratch (allocated on first solve, grown on demand)
   size_t gm_bytes = 0;

@@ -15,19 +15,10 @@
 // 768, 1536 and 1024 tasks for 256 threads).
 #pragma once
 
+#include "fastpath.cuh"
 #include "matvec4.cuh"
 
 namespace marie {
-
-__host__ __device__ constexpr int kz4_stride(int N, int W) { return N + (W >= 16 ? 1 : 16 / W); }
-__host__ __device__ constexpr int kz4_halfpad(int W) { return W >= 16 ? 0 : 8 / W; }
-
-// Shared-memory bytes of k4_z: twiddles + both halves.
-template <typename T>
-__host__ inline size_t kz4_smem(int N, int C, int W) {
-  const size_t half = (size_t)C * W * kz4_stride(N, W);
-  return (N + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
-}
 
 __device__ __forceinline__ int zpos(int j, int k1) { return j * 16 + (k1 ^ j); }
 
@@ -36,6 +27,10 @@ __device__ __forceinline__ cplx<float> shfl_xor_c(cplx<float> v, int m) {
 }
 __device__ __forceinline__ cplx<double> shfl_xor_c(cplx<double> v, int m) {
   return {__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+}
+__device__ __forceinline__ cplx<ff> shfl_xor_c(cplx<ff> v, int m) {
+  return {ff(__shfl_xor_sync(0xffffffffu, v.x.hi, m), __shfl_xor_sync(0xffffffffu, v.x.lo, m)),
+          ff(__shfl_xor_sync(0xffffffffu, v.y.hi, m), __shfl_xor_sync(0xffffffffu, v.y.lo, m))};
 }
 
 // One entry of the single-point Green multiply (entries sorted by block;

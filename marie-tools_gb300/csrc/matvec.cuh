@@ -72,8 +72,8 @@ struct MvArgs {
   const int* vox2sol;         // n1*n2*n3 -> body index or -1
   const cplx<T>* chi;         // contrast (Mc/Mr) per body voxel
   T invg[kMaxComp];           // invG diagonal per component
-  const cplx<T>* in;          // rhs r at in + r*in_rs
-  cplx<T>* out;
+  const cplx<typename IoOf<T>::type>* in;   // rhs r at in + r*in_rs
+  cplx<typename IoOf<T>::type>* out;
   int64_t in_rs, out_rs;      // element stride between right-hand sides
   cplx<T>* T1;                // [bundle][c][z][y][2n1][R]
   cplx<T>* S;                 // [bundle][c][2n2][z][2n1][R]

@@ -94,7 +94,7 @@ __device__ __forceinline__ void dftn(cplx<T>* v) {
 // buf: sequence s = (yy*R + r)*2 + alpha, stride S = 16*NB + 1, [k1][b]
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256, 3) k4_fwd_x(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_x(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(256, 3) k4_fwd_x(MvArgs<T> a) {
     const int r = rr & (R - 1), yy = rr >> lgR;
     const int rhs = bu * R + r;
     const bool act = lane_active(a, rhs);
-    const cplx<T>* in = a.in + (int64_t)rhs * a.in_rs;
+    const auto* in = a.in + (int64_t)rhs * a.in_rs;
     const int64_t grow = (int64_t)N * (y0 + yy + (int64_t)n2 * z);
     cplx<T> v[16], u[16];
 #pragma unroll
@@ -122,11 +122,11 @@ __global__ void __launch_bounds__(256, 3) k4_fwd_x(MvArgs<T> a) {
       cplx<T> val = {0, 0};
       if (act) {
         if (a.mode == MV_GRID) {
-          val = in[(int64_t)c * nD + grow + x];
+          val = io_load<T>(in[(int64_t)c * nD + grow + x]);
         } else {
           const int s = a.vox2sol[grow + x];
           if (s >= 0) {
-            val = in[(int64_t)c * a.Ns + s];
+            val = io_load<T>(in[(int64_t)c * a.Ns + s]);
             if (a.mode == MV_VIE_ADJ) val = scale(mulc(val, a.chi[s]), a.invg[c]);
           }
         }
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256, 3) k4_fwd_x(MvArgs<T> a) {
 // Pass XI (inverse x + crop + epilogue), n1 = 16*NB.
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256, 3) k4_inv_x(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_x(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -216,14 +216,14 @@ __global__ void __launch_bounds__(256, 3) k4_inv_x(MvArgs<T> a) {
       const int x = NB * q + b;
       cplx<T> v = u0[q] + mulc(u1[q], a.ax.tw2[x]);
       if (a.mode == MV_GRID) {
-        a.out[(int64_t)rhs * a.out_rs + (int64_t)c * nD + grow + x] = v;
+        a.out[(int64_t)rhs * a.out_rs + (int64_t)c * nD + grow + x] = io_store(v);
       } else {
         const int s = a.vox2sol[grow + x];
         if (s >= 0) {
           const int64_t o = (int64_t)c * a.Ns + s;
-          const cplx<T> xin = a.in[(int64_t)rhs * a.in_rs + o];
+          const cplx<T> xin = io_load<T>(a.in[(int64_t)rhs * a.in_rs + o]);
           if (a.mode == MV_VIE) v = scale(a.chi[s] * v, a.invg[c]);
-          a.out[(int64_t)rhs * a.out_rs + o] = xin - v;
+          a.out[(int64_t)rhs * a.out_rs + o] = io_store(xin - v);
         }
       }
     }
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(256, 3) k4_inv_x(MvArgs<T> a) {
 // buf: sequence s = beta*W + e, stride S, [k1][b]
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256, 3) k4_fwd_y(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_y(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(256, 3) k4_fwd_y(MvArgs<T> a) {
 // Pass YI (inverse y + crop), n2 = 16*NB.
 // ---------------------------------------------------------------------------
 template <typename T, int NB>
-__global__ void __launch_bounds__(256, 3) k4_inv_y(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB, S = N + 1;
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;

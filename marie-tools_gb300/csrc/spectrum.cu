@@ -167,7 +167,7 @@ static marie_status check_parity_tucker(const marie_tucker_block& t, int n1, int
 
 // Build all blocks of one operator (N or K) into the handle's spectra.
 static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const double* dense, int ncomp,
-                             cplx<double>* dst64, cplx<float>* dst32) {
+                             cplx<double>* dst64, cplx<float>* dst32, cplx<ff>* dstff) {
   const int n1 = h->n1, n2 = h->n2, n3 = h->n3;
   const int pwx = h->pwl ? 10 : 1;
   const int nblk = pwx * ncomp;
@@ -237,6 +237,7 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
         g_launches++;
         if (dst64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
         if (dst32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        if (dstff) { k_oct_store<ff><<<grid_for(oct), 256>>>(tmp, dstff + id * oct, nkx, nky, nkz, scl); g_launches++; }
         if (cudaGetLastError() != cudaSuccess) { set_error("spectrum kernel launch failed"); st = MARIE_ERR_CUDA; break; }
         cudaDeviceSynchronize();
       }
@@ -278,6 +279,7 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
         g_launches++;
         if (dst64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
         if (dst32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        if (dstff) { k_oct_store<ff><<<grid_for(oct), 256>>>(tmp, dstff + id * oct, nkx, nky, nkz, scl); g_launches++; }
         if (cudaGetLastError() != cudaSuccess) { set_error("spectrum kernel launch failed"); st = MARIE_ERR_CUDA; break; }
         cudaDeviceSynchronize();
       }
@@ -297,8 +299,13 @@ marie_status build_spectra(marie_vie* h, const marie_vie_desc* d) {
     MARIE_TRY(dev_alloc(h, (void**)&h->p32.GN, (size_t)h->nblkN * oct * sizeof(cplx<float>)));
     if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->p32.GK, (size_t)h->nblkK * oct * sizeof(cplx<float>)));
   }
-  MARIE_TRY(build_op(h, d->tucker_N, d->tucker_N ? nullptr : d->dense_N, 6, h->p64.GN, h->p32.GN));
-  if (h->has_K) MARIE_TRY(build_op(h, d->tucker_K, d->tucker_K ? nullptr : d->dense_K, 3, h->p64.GK, h->p32.GK));
+  if (h->precisions & 4) {
+    MARIE_TRY(dev_alloc(h, (void**)&h->pff.GN, (size_t)h->nblkN * oct * sizeof(cplx<ff>)));
+    if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->pff.GK, (size_t)h->nblkK * oct * sizeof(cplx<ff>)));
+  }
+  MARIE_TRY(build_op(h, d->tucker_N, d->tucker_N ? nullptr : d->dense_N, 6, h->p64.GN, h->p32.GN, h->pff.GN));
+  if (h->has_K)
+    MARIE_TRY(build_op(h, d->tucker_K, d->tucker_K ? nullptr : d->dense_K, 3, h->p64.GK, h->p32.GK, h->pff.GK));
   return MARIE_OK;
 }
 

@@ -30,8 +30,19 @@ def _nvcc() -> str:
     return cand
 
 
+# Sources compiled more than once with different macros: one object each.
+# The float-float z-pass kernels are split by NB = n3/16 so that the eight
+# objects compile in parallel (together they take many minutes).
+VARIANTS = {"fast_ff_z.cu": [(f"fast_ff_z{nb}", [f"-DMARIE_FF_NB={nb}"]) for nb in range(1, 9)]}
+
+
 def _sources():
-    return sorted(CSRC.glob("*.cu"))
+    """(source, object stem, extra flags) of every object in the library."""
+    out = []
+    for src in sorted(CSRC.glob("*.cu")):
+        for stem, extra in VARIANTS.get(src.name, [(src.stem, [])]):
+            out.append((src, stem, extra))
+    return out
 
 
 def _stamp() -> str:
@@ -55,9 +66,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     objdir = LIBDIR / "obj"
     objdir.mkdir(exist_ok=True)
 
-    def compile_one(src: Path) -> Path:
-        obj = objdir / (src.stem + ".o")
-        cmd = [nvcc, *ARCH, *FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+    def compile_one(item) -> Path:
+        src, stem, extra = item
+        obj = objdir / (stem + ".o")
+        cmd = [nvcc, *ARCH, *FLAGS, *extra, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stderr}")
@@ -67,7 +79,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(compile_one, srcs))
+        # the four-step kernel units are the slowest: start them first
+        order = sorted(srcs, key=lambda it: (not it[1].startswith("fast"), it[1]))
+        objs = list(ex.map(compile_one, order))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

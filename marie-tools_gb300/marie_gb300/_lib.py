@@ -20,6 +20,9 @@ STATUS_NAMES = {0: "MARIE_OK", 1: "MARIE_ERR_BAD_ARG", 2: "MARIE_ERR_OOM", 3: "M
                 4: "MARIE_ERR_NOT_CONVERGED", 5: "MARIE_ERR_DEVICE_TIMEOUT", 6: "MARIE_ERR_CUDA",
                 7: "MARIE_ERR_NOT_SUPPORTED"}
 C128, C64 = 0, 1
+# marie_vie_desc.precisions bits: native complex128, complex64, complex128 with
+# float-float arithmetic (grid edges 16*NB, NB <= 8; exclusive with bit 1)
+PREC_C128, PREC_C64, PREC_C128FF = 1, 2, 4
 PWC, PWL = 0, 1
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 

@@ -48,6 +48,11 @@ class VieOperator:
     and the N (and optionally K) operator either as Tucker blocks
     {(j, k): (G, U1, U2, U3)} (assembly_fft_circ_tucker_*.m output) or as a
     dense I_V array (n1, n2, n3, pwx, 6|3).
+
+    ``precisions`` is a bit mask of the device states to build: 1 native
+    complex128, 2 complex64, 4 complex128 evaluated in float-float arithmetic
+    (grid edges 16*NB with NB <= 8, N and N^H only; exclusive with 1).
+    complex128 calls run on whichever complex128 state was built.
     """
 
     def __init__(self, dims, res, freq, idx_solution, Mr, N, K=None, *, pwl: bool,
@@ -171,7 +176,7 @@ class VieOperator:
     def tiles(self, prec=C64):
         out = np.zeros(4, np.int32)
         check(self._lib.marie_vie_tiles(self._h, prec, out.ctypes.data_as(_lib.c_int32_p)))
-        return dict(chunk=int(out[0]), width=int(out[1]))
+        return dict(chunk=int(out[0]), width=int(out[1]), float_float=bool(out[2]))
 
     # -- solve ----------------------------------------------------------------
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,

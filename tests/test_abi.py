@@ -63,6 +63,8 @@ def test_rejects_bad_descriptors(lib):
         dict(base, res=-1.0),
         dict(base, freq=0.0),
         dict(base, precisions=0),
+        dict(base, precisions=8),
+        dict(base, precisions=5),                # native and float-float complex128 together
         dict(base, max_rhs=0),
         dict(base, n_b=16),                      # not a multiple of 3
         dict(base),                              # idx_solution not component-major
@@ -73,6 +75,18 @@ def test_rejects_bad_descriptors(lib):
         assert st == 1, (kw.keys(), st, _lib.last_error())
         assert not h.value
         assert _lib.last_error()
+
+
+def test_float_float_needs_four_step_grid(lib):
+    """precisions bit 4 (complex128 in float-float arithmetic) is offered on
+    grids whose edges are 16*NB with NB <= 8 only."""
+    idx = np.arange(3 * 5, dtype=np.int64)
+    mr = np.ones(2 * 64)
+    dense = np.zeros(2 * 64 * 6)
+    d = _desc(n_b=15, idx_solution=idx.ctypes.data_as(ct.POINTER(ct.c_int64)), precisions=6,
+              Mr=mr.ctypes.data_as(_lib.c_double_p), dense_N=dense.ctypes.data_as(_lib.c_double_p))
+    st, h = _create(lib, d)
+    assert st == 7 and not h.value and "16*NB" in _lib.last_error()
 
 
 def test_rejects_out_of_grid_index(lib):
