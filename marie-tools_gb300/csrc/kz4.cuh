@@ -72,8 +72,110 @@ __device__ __forceinline__ void zpoint(std::integer_sequence<int, Ks...>, cplx<T
   for (int p = 0; p < C; ++p) v[p * qstride] = y[p];
 }
 
+// ---------------------------------------------------------------------------
+// Float-float PWL multiply of one point for N / N^H.  Unrolled like zpoint,
+// the 144 entries are ~7k instructions in float-float and overflow the
+// instruction cache, so here the input group Q runs as a loop (three trips)
+// over a body holding the output groups P and the ten Tucker indices j
+// unrolled: block (j, k) with k = PQ_N(P, Q) - 1, entries (l, lp) with
+// |LLP(l, lp)| = j + 1 (the same for every (P, Q) since PQ_N carries no sign).
+// Accumulators stay unnormalised (hi, lo) pairs until the end.
+// ---------------------------------------------------------------------------
+struct PwlPQ {
+  int jl[4][4];          // Tucker index j of entry (l, lp)
+  int sg[4][4];          // its sign
+  unsigned gmask[3];     // per axis: bits k whose circulant sign is negative (j = 0)
+  unsigned bmask[3];     // per axis: bits j whose sign is negative (k = 0)
+};
+
+template <int OP>
+constexpr PwlPQ make_pwl_pq() {
+  using Tab = OpTab<true, OP>;
+  PwlPQ t{};
+  for (int i = 0; i < Tab::NE; ++i) {
+    const OpEntry e = Tab::L.e[i];
+    if (e.p < 4 && e.q < 4) {      // (P, Q) = (0, 0): block (j, 0)
+      t.jl[e.p][e.q] = e.blk / 6;
+      t.sg[e.p][e.q] = e.sgn;
+    }
+  }
+  for (int ax = 0; ax < 3; ++ax) {
+    const int* s = ax == 0 ? Tab::L.s1 : (ax == 1 ? Tab::L.s2 : Tab::L.s3);
+    unsigned g = 0, b = 0;
+    for (int k = 0; k < 6; ++k) g |= (s[k] < 0 ? 1u : 0u) << k;
+    for (int j = 0; j < 10; ++j) b |= (s[6 * j] < 0 ? 1u : 0u) << j;
+    t.gmask[ax] = g;
+    t.bmask[ax] = b;
+  }
+  return t;
+}
+
+// acc += sgn * a * b on unnormalised float-float pairs (product error by FMA,
+// sum error by two-sum, both collected in acc.lo)
+template <int SG>
+__device__ __forceinline__ void ff_acc(ff& acc, ff a, ff b) {
+  const float ah = SG > 0 ? a.hi : -a.hi, al = SG > 0 ? a.lo : -a.lo;
+  const float p = __fmul_rn(ah, b.hi);
+  float e = __fmaf_rn(ah, b.hi, -p);
+  e = __fmaf_rn(ah, b.lo, e);
+  e = __fmaf_rn(al, b.hi, e);
+  const ff s = ff_two_sum(acc.hi, p);
+  acc.hi = s.hi;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(s.lo, e));
+}
+
+template <int SG>
+__device__ __forceinline__ void ff_cmac(cplx<ff>& y, cplx<ff> g, cplx<ff> x) {
+  ff_acc<SG>(y.x, g.x, x.x);
+  ff_acc<-SG>(y.x, g.y, x.y);
+  ff_acc<SG>(y.y, g.x, x.y);
+  ff_acc<SG>(y.y, g.y, x.x);
+}
+
+template <int OP>
+__device__ __forceinline__ void zpoint_pwl_ff(cplx<ff>* v, int qstride, const cplx<ff>* gp, int64_t gblk, bool mx,
+                                              bool my, bool mz) {
+  constexpr PwlPQ TB = make_pwl_pq<OP>();
+  const unsigned fk = (mx ? TB.gmask[0] : 0u) ^ (my ? TB.gmask[1] : 0u) ^ (mz ? TB.gmask[2] : 0u);
+  const unsigned fj = (mx ? TB.bmask[0] : 0u) ^ (my ? TB.bmask[1] : 0u) ^ (mz ? TB.bmask[2] : 0u);
+  cplx<ff> y[12];
+#pragma unroll
+  for (int p = 0; p < 12; ++p) y[p] = cplx<ff>{0, 0};
+#pragma unroll 1
+  for (int Q = 0; Q < 3; ++Q) {
+    cplx<ff> x[4];
+#pragma unroll
+    for (int lp = 0; lp < 4; ++lp) x[lp] = v[(4 * Q + lp) * qstride];
+#pragma unroll
+    for (int P = 0; P < 3; ++P) {
+      const int k = P + Q + ((P > 0 && Q > 0) ? 1 : 0);    // PQ_N(P, Q) - 1
+      const cplx<ff>* gk = gp + k * gblk;
+      const unsigned fkb = (fk >> k) & 1u;
+#pragma unroll
+      for (int j = 0; j < 10; ++j) {
+        cplx<ff> g = ldg_c(gk + (int64_t)(6 * j) * gblk);
+        if constexpr ((OP & 1) != 0) g = conjg(g);
+        if ((fkb ^ (fj >> j)) & 1u) g = cplx<ff>{-g.x, -g.y};
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+#pragma unroll
+          for (int lp = 0; lp < 4; ++lp) {
+            if (TB.jl[l][lp] == j) {
+              if (TB.sg[l][lp] > 0) ff_cmac<1>(y[4 * P + l], g, x[lp]);
+              else ff_cmac<-1>(y[4 * P + l], g, x[lp]);
+            }
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < 12; ++p)
+    v[p * qstride] = cplx<ff>{ff_fast_two_sum(y[p].x.hi, y[p].x.lo), ff_fast_two_sum(y[p].y.hi, y[p].y.lo)};
+}
+
 template <typename T, int NB, bool PWL, int OP>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k4_z(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::value) ? 2 : 1) k4_z(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB;
   constexpr int C = PWL ? 12 : 3;
@@ -149,8 +251,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k4_z(MvArgs<T> a)
     const bool mx = kx > n1;
     const int kxo = mx ? 2 * n1 - kx : kx;
     const cplx<T>* gp = a.G + ((int64_t)kyo * (n1 + 1) + kxo) * nko + kzo;
-    zpoint<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, buf + g * H + e * S + zpos(k >> 4, k & 15), W * S,
-                       gp, gblk, mx, my, mz);
+    cplx<T>* v = buf + g * H + e * S + zpos(k >> 4, k & 15);
+    if constexpr (PWL && std::is_same<T, ff>::value && OP <= 1)
+      zpoint_pwl_ff<OP>(v, W * S, gp, gblk, mx, my, mz);
+    else
+      zpoint<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, v, W * S, gp, gblk, mx, my, mz);
   }
   __syncthreads();
   // inverse step A (in place): task (s, k1), k1 fastest
