@@ -357,6 +357,12 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   fill_axis(a.ay, ps.ay);
   fill_axis(a.az, ps.az);
   a.vox2sol = h->vox2sol;
+  if (mode != MV_GRID && !env_int("MARIE_NO_PRUNE", 0)) {
+    a.row_live = h->row_live;
+    a.z_live = h->z_live;
+    a.rowq = h->rowq;
+    a.zq = h->zq;
+  }
   a.chi = ps.chi;
   for (int c = 0; c < h->C; ++c) a.invg[c] = prec_from<T>(h->invg[c]);
   a.T1 = ps.T1;
@@ -523,6 +529,37 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   if (cudaMemcpy(h->vox2sol, vox.data(), nD * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
     set_error("upload of the body map failed");
     return fail(MARIE_ERR_CUDA);
+  }
+  {
+    std::vector<unsigned char> rl((size_t)h->n2 * h->n3, 0), zl(h->n3, 0);
+    for (int64_t s = 0; s < h->Ns; ++s) {
+      const int64_t yz = idxS[s] / h->n1;          // y + n2*z
+      rl[yz] = 1;
+      zl[yz / h->n2] = 1;
+    }
+    if ((st = dev_alloc(h, (void**)&h->row_live, rl.size())) != MARIE_OK) return fail(st);
+    if ((st = dev_alloc(h, (void**)&h->z_live, zl.size())) != MARIE_OK) return fail(st);
+    cudaMemcpy(h->row_live, rl.data(), rl.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(h->z_live, zl.data(), zl.size(), cudaMemcpyHostToDevice);
+    if (four_step_edge(h->n2)) {
+      const int nb = h->n2 / 16;
+      std::vector<uint16_t> rq((size_t)h->n3 * 8, 0);
+      for (int z = 0; z < h->n3; ++z)
+        for (int b = 0; b < nb; ++b)
+          for (int q = 0; q < 16; ++q)
+            if (rl[(size_t)z * h->n2 + nb * q + b]) rq[(size_t)z * 8 + b] |= (uint16_t)(1u << q);
+      if ((st = dev_alloc(h, (void**)&h->rowq, rq.size() * sizeof(uint16_t))) != MARIE_OK) return fail(st);
+      cudaMemcpy(h->rowq, rq.data(), rq.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+    }
+    if (four_step_edge(h->n3)) {
+      const int nb = h->n3 / 16;
+      std::vector<uint16_t> zq(8, 0);
+      for (int b = 0; b < nb; ++b)
+        for (int q = 0; q < 16; ++q)
+          if (zl[nb * q + b]) zq[b] |= (uint16_t)(1u << q);
+      if ((st = dev_alloc(h, (void**)&h->zq, zq.size() * sizeof(uint16_t))) != MARIE_OK) return fail(st);
+      cudaMemcpy(h->zq, zq.data(), zq.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+    }
   }
   if ((st = dev_alloc(h, (void**)&h->idxS, h->Ns * sizeof(int64_t))) != MARIE_OK) return fail(st);
   cudaMemcpy(h->idxS, idxS.data(), h->Ns * sizeof(int64_t), cudaMemcpyHostToDevice);

@@ -75,6 +75,10 @@ struct marie_vie {
   int64_t mem_cap = 0, mem_used = 0;
   double invg[12] = {0};
   int* vox2sol = nullptr;            // device, n1*n2*n3
+  unsigned char* row_live = nullptr; // device, n2*n3: grid row (y, z) holds a body voxel
+  unsigned char* z_live = nullptr;   // device, n3: slice z holds a body voxel
+  uint16_t* rowq = nullptr;          // device, n3*8: row_live in four-step order (n2 = 16*NB)
+  uint16_t* zq = nullptr;            // device, 8: z_live in four-step order (n3 = 16*NB)
   int64_t* idxS = nullptr;           // device, Ns (0-based linear voxel index)
   std::vector<int64_t> idxS_host;
   marie::BlockTab tab[4];            // N, N_adj, K, K_adj

@@ -203,10 +203,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
     const int e = t % W, r = t / W;
     const int h = r & 1, r2 = r >> 1;
     const int b = r2 % NB, c = r2 / NB;
+    const unsigned live = a.zq ? a.zq[b] : 0xffffu;   // slices z = NB*q + b
     cplx<T> u[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      cplx<T> val = e < wl ? base[c * cstride + (int64_t)(NB * q + b) * row + e] : cplx<T>{0, 0};
+      cplx<T> val = (e < wl && ((live >> q) & 1u)) ? base[c * cstride + (int64_t)(NB * q + b) * row + e]
+                                                   : cplx<T>{0, 0};
       if (h) val = val * a.az.tw2[NB * q + b];
       u[q] = val;
     }
@@ -295,13 +297,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
       for (int q = 0; q < 16; ++q) u[q] = mulc(u[q], a.az.tw2[NB * q + b]);
     }
     const bool st = act && e < wl;
+    const unsigned live = (a.zq ? a.zq[b] : 0xffffu) >> (8 * h);   // slices z = NB*(8h + j) + b
     cplx<T>* dst = base + c * cstride + (int64_t)(NB * 8 * h + b) * row + e;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const cplx<T> send = h ? u[j] : u[8 + j];
       const cplx<T> recv = shfl_xor_c(send, W);
       const cplx<T> out = h ? recv + u[8 + j] : u[j] + recv;
-      if (st) dst[(int64_t)NB * j * row] = out;
+      if (st && ((live >> j) & 1u)) dst[(int64_t)NB * j * row] = out;
     }
   }
 }

@@ -79,6 +79,17 @@ struct MvArgs {
   cplx<T>* S;                 // [bundle][c][2n2][z][2n1][R]
   const cplx<T>* G;           // octant spectra [blk][n2+1][n1+1][n3+1]
   const unsigned char* active;  // per rhs: nonzero = process (may be null)
+  // Body occupancy for the pruned four-step passes (null: every row live).
+  // row_live[z*n2 + y]: the grid row (y, z) holds a body voxel; z_live[z]:
+  // slice z does.  Rows and slices that are not live are zero on input and
+  // not needed on output, so the passes neither transform nor store them.
+  const unsigned char* row_live;
+  const unsigned char* z_live;
+  // The same occupancy in the four-step index order (edges 16*NB): bit q of
+  // rowq[z*8 + b] is row y = NB*q + b of slice z, bit q of zq[b] is slice
+  // z = NB*q + b (null: all live).
+  const uint16_t* rowq;
+  const uint16_t* zq;
   int TY, TXY, TX;            // tile sizes of the X, Y, Z passes
 };
 
@@ -90,6 +101,16 @@ __device__ __forceinline__ void load_tw(cplx<T>* dst, const cplx<T>* src, int n)
 template <typename T>
 __device__ __forceinline__ bool lane_active(const MvArgs<T>& a, int rhs) {
   return rhs < a.nrhs && (a.active == nullptr || a.active[rhs]);
+}
+
+template <typename T>
+__device__ __forceinline__ bool row_is_live(const MvArgs<T>& a, int y, int z) {
+  return a.row_live == nullptr || a.row_live[z * a.n2 + y] != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ bool z_is_live(const MvArgs<T>& a, int z) {
+  return a.z_live == nullptr || a.z_live[z] != 0;
 }
 
 template <typename T>

@@ -102,6 +102,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_x(MvArgs<T
   const int z = blockIdx.y, y0 = blockIdx.x * a.TY;
   const int n2 = a.n2, n3 = a.n3, R = a.R, lgR = a.lgR;
   const int ty = min(a.TY, n2 - y0);
+  bool any = false;
+  for (int yy = 0; yy < ty; ++yy) any = any || row_is_live(a, y0 + yy, z);
+  if (!any) return;   // rows without body voxels stay unwritten: the y pass reads them as zero
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + N;
   load_tw(tw, a.ax.tw, N);
@@ -111,6 +114,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_x(MvArgs<T
   for (int t = threadIdx.x; t < ty * R * NB; t += blockDim.x) {
     const int b = t % NB, rr = t / NB;
     const int r = rr & (R - 1), yy = rr >> lgR;
+    if (!row_is_live(a, y0 + yy, z)) continue;
     const int rhs = bu * R + r;
     const bool act = lane_active(a, rhs);
     const auto* in = a.in + (int64_t)rhs * a.in_rs;
@@ -151,6 +155,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_x(MvArgs<T
   for (int t = threadIdx.x; t < ty * 32 * R; t += blockDim.x) {
     const int r = t & (R - 1), q = t >> lgR;
     const int k1 = q & 15, alpha = (q >> 4) & 1, yy = q >> 5;
+    if (!row_is_live(a, y0 + yy, z)) continue;
     const cplx<T>* src = buf + ((yy * R + r) * 2 + alpha) * S + k1 * NB;
     cplx<T> w[NB];
 #pragma unroll
@@ -174,6 +179,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_x(MvArgs<T
   const int z = blockIdx.y, y0 = blockIdx.x * a.TY;
   const int n2 = a.n2, n3 = a.n3, R = a.R, lgR = a.lgR;
   const int ty = min(a.TY, n2 - y0);
+  bool any = false;
+  for (int yy = 0; yy < ty; ++yy) any = any || row_is_live(a, y0 + yy, z);
+  if (!any) return;   // no body voxel in these rows: no output
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + N;
   load_tw(tw, a.ax.tw, N);
@@ -184,6 +192,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_x(MvArgs<T
   for (int t = threadIdx.x; t < ty * 32 * R; t += blockDim.x) {
     const int r = t & (R - 1), q = t >> lgR;
     const int k1 = q & 15, alpha = (q >> 4) & 1, yy = q >> 5;
+    if (!row_is_live(a, y0 + yy, z)) continue;
     const cplx<T>* in = srow + (int64_t)(y0 + yy) * rowlen + (alpha * N + k1) * R + r;
     cplx<T> w[NB];
 #pragma unroll
@@ -200,7 +209,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_x(MvArgs<T
     const int b = t % NB, rr = t / NB;
     const int r = rr & (R - 1), yy = rr >> lgR;
     const int rhs = bu * R + r;
-    if (!lane_active(a, rhs)) continue;
+    if (!lane_active(a, rhs) || !row_is_live(a, y0 + yy, z)) continue;
     const cplx<T>* s0 = buf + ((yy * R + r) * 2) * S + b;
     cplx<T> u0[16], u1[16];
 #pragma unroll
@@ -241,6 +250,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_y(MvArgs<T
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
   if (!bundle_active(a, bu)) return;
   const int z = blockIdx.y, k0 = blockIdx.x * a.TXY;
+  if (!z_is_live(a, z)) return;   // slice without body voxels: the z pass reads it as zero
   const int n1 = a.n1, n3 = a.n3, m1 = 2 * n1, R = a.R;
   const int W = a.TXY * R, wl = min(a.TXY, m1 - k0) * R;
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -252,10 +262,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_y(MvArgs<T
   // step 1: task (b, e), e fastest
   for (int t = threadIdx.x; t < W * NB; t += blockDim.x) {
     const int e = t % W, b = t / W;
+    const unsigned live = a.rowq ? a.rowq[z * 8 + b] : 0xffffu;   // rows y = NB*q + b
     cplx<T> v[16], u[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      const cplx<T> val = e < wl ? src[(int64_t)(NB * q + b) * row + e] : cplx<T>{0, 0};
+      const cplx<T> val =
+          (e < wl && ((live >> q) & 1u)) ? src[(int64_t)(NB * q + b) * row + e] : cplx<T>{0, 0};
       v[q] = val;
       u[q] = val;
     }
@@ -295,6 +307,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
   const int bc = blockIdx.z, bu = bc / a.C, c = bc - bu * a.C;
   if (!bundle_active(a, bu)) return;
   const int z = blockIdx.y, k0 = blockIdx.x * a.TXY;
+  if (!z_is_live(a, z)) return;   // no body voxel in slice z: no output
   const int n1 = a.n1, n3 = a.n3, m1 = 2 * n1, R = a.R;
   const int W = a.TXY * R, wl = min(a.TXY, m1 - k0) * R;
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -320,6 +333,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
   cplx<T>* dst = a.T1 + (((int64_t)bu * a.C + c) * n3 + z) * (int64_t)N * row + (int64_t)k0 * R;
   for (int t = threadIdx.x; t < W * NB; t += blockDim.x) {
     const int e = t % W, b = t / W;
+    const unsigned live = a.rowq ? a.rowq[z * 8 + b] : 0xffffu;   // rows y = NB*q + b
     cplx<T> u0[16], u1[16];
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) {
@@ -332,7 +346,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
         const int y = NB * q + b;
-        dst[(int64_t)y * row + e] = u0[q] + mulc(u1[q], a.ay.tw2[y]);
+        if ((live >> q) & 1u) dst[(int64_t)y * row + e] = u0[q] + mulc(u1[q], a.ay.tw2[y]);
       }
     }
   }

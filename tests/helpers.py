@@ -6,11 +6,19 @@ import numpy as np
 from oracle import marie_oracle as O
 
 
-def random_body(n, seed, density=0.6):
+def random_body(n, seed, density=0.6, box=None):
+    """Random voxel body; box = ((x0, x1), (y0, y1), (z0, z1)) keeps it inside
+    that sub-box (grid rows and slices outside it hold no body voxel)."""
     rng = np.random.default_rng(seed)
     n1, n2, n3 = n
     mask = rng.uniform(size=(n1, n2, n3)) < density
-    mask[0, 0, 0] = True
+    if box is None:
+        mask[0, 0, 0] = True
+    else:
+        keep = np.zeros_like(mask)
+        keep[box[0][0]:box[0][1], box[1][0]:box[1][1], box[2][0]:box[2][1]] = True
+        mask &= keep
+        mask[box[0][0], box[1][0], box[2][0]] = True
     idxS = np.nonzero(mask.reshape(-1, order="F"))[0].astype(np.int64)
     er = np.where(mask, rng.uniform(5, 80, size=(n1, n2, n3)), 1.0)
     se = np.where(mask, rng.uniform(0.02, 2.0, size=(n1, n2, n3)), 0.0)
@@ -46,11 +54,12 @@ def synthetic_IV(n, pwl, kernel, seed):
 class Problem:
     """Operator data of one small case, in the reference's formats."""
 
-    def __init__(self, n, pwl, seed=0, res=5e-3, freq=128e6, tucker_tol=1e-14, physical=False, iv_scale=1.0):
+    def __init__(self, n, pwl, seed=0, res=5e-3, freq=128e6, tucker_tol=1e-14, physical=False, iv_scale=1.0,
+                 box=None):
         self.n = tuple(n)
         self.pwl = pwl
         self.res, self.freq = res, freq
-        self.idxS, self.er, self.se = random_body(n, seed)
+        self.idxS, self.er, self.se = random_body(n, seed, box=box)
         self.emc = O.em_constants(freq)
         ep = O.em_assembly(self.er, self.se, self.emc["ce"])
         self.Mr, self.Mc = ep["Mr"], ep["Mc"]

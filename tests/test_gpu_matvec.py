@@ -178,3 +178,40 @@ def test_four_step_path(n, pwl, prec, monkeypatch):
     for r in range(5):
         assert rel_err(yb[r], O.mvp_vie(X[r], P.Mr, P.Mc, P.dims, P.TN, cache={})) <= TOL[prec]
     op.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
+@pytest.mark.parametrize("precisions,prec", [(3, "c128"), (3, "c64"), (6, "c128")], ids=["c128", "c64", "c128ff"])
+def test_pruned_passes_on_a_partial_body(pwl, precisions, prec, monkeypatch):
+    """A body inside a sub-box leaves grid rows and z slices without body
+    voxels: the four-step passes skip them (inputs are zero there, outputs
+    are not needed).  Results equal the unpruned passes and the oracle."""
+    n = (32, 16, 48)
+    P = Problem(n, pwl, seed=31 + pwl, box=((3, 21), (2, 11), (6, 40)))
+    # a hole: slices 15..19 and rows y = 5 hold no body voxel either
+    keep = []
+    for s_ in P.idxS:
+        x, r = s_ % n[0], s_ // n[0]
+        y, z = r % n[1], r // n[1]
+        keep.append(not (15 <= z < 20 or y == 5))
+    P2 = Problem.__new__(Problem)
+    P2.__dict__.update(P.__dict__)
+    P2.idxS = P.idxS[np.array(keep)]
+    P2.dims = O.geo_dims(*n, P2.idxS, pwl, P.res)
+    op = P2.gpu_operator(precisions=precisions, max_rhs=4)
+    X = P2.random_body_vec(seed=2, nrhs=3)
+    x = torch.from_numpy(X.reshape(-1)).to("cuda", _dt(prec))
+    y = op.apply(x).cpu().numpy()
+    ya = op.apply_adjoint(x).cpu().numpy()
+    monkeypatch.setenv("MARIE_NO_PRUNE", "1")
+    yu = op.apply(x).cpu().numpy()
+    yau = op.apply_adjoint(x).cpu().numpy()
+    monkeypatch.delenv("MARIE_NO_PRUNE")
+    assert np.array_equal(y, yu) and np.array_equal(ya, yau)
+    tol = 1e-11 if precisions == 6 else TOL[prec]
+    y = y.reshape(3, -1).astype(np.complex128)
+    for r in range(3):
+        ref = O.mvp_vie(X[r], P2.Mr, P2.Mc, P2.dims, P2.TN, cache={})
+        assert rel_err(y[r], ref) <= tol
+    op.close()
