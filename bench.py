@@ -136,13 +136,15 @@ def build_problem(wl, rank, torch):
     return op, body, b.reshape(-1), t_asm
 
 
-def roofline_z(op, wl, tiles, ms_z, peak, peak_kind):
-    """Algorithmic bytes of one z-pass launch / its event-timed duration."""
+def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
+    """Algorithmic bytes of one z-pass launch / its event-timed duration.
+    zfrac: fraction of z slices holding body voxels (the pass reads and
+    writes those only)."""
     n, C = wl["n"], 12 if wl["pwl"] else 3
     U = 60 if wl["pwl"] else 6
     s = 8                                   # complex64
     units = min(tiles["chunk"], wl["nrhs"])  # right-hand sides per launch
-    per_rhs = 8 * n ** 3 * C * s            # read + write 4 n^3 per component
+    per_rhs = 8 * n ** 3 * C * s * zfrac    # read + write 4 n^3 per component (live slices)
     green = U * (n + 1) ** 3 * s            # octant spectrum, read once per launch
     alg = units * per_rhs + green
     achieved = alg / (ms_z * 1e-3) / 1e9
@@ -154,7 +156,7 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind):
     name = (f"k4_z<float,{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
     return {"kernel": name + " (z FFT + Green block multiply + inverse z FFT)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-            "traffic": traffic, "alg_bytes_per_launch": alg, "launch_ms": round(ms_z, 4),
+            "traffic": traffic, "alg_bytes_per_launch": int(alg), "launch_ms": round(ms_z, 4),
             "units_per_launch": units, "peak_source": peak_kind}
 
 
@@ -225,7 +227,9 @@ def run_ours(args, wl):
     tiles = op.tiles()
     xs = b[: op.Nb * min(nrhs, tiles["chunk"])].to(torch.complex64)
     passes = op.profile(xs, reps=5)
-    roof = roofline_z(op, wl, tiles, passes[2], peak, peak_kind)
+    zlive = np.unique(body.idxS // (body.n[0] * body.n[1])).size / body.n[2]
+    roof = roofline_z(op, wl, tiles, passes[2], peak, peak_kind, zfrac=zlive)
+    roof["live_z_fraction"] = round(float(zlive), 4)
     n, C, s = wl["n"], 12 if wl["pwl"] else 3, 8
     U = 60 if wl["pwl"] else 6
     units = xs.numel() // op.Nb

@@ -57,7 +57,7 @@ marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaS
   const size_t smz = kz4_smem<T>(n3, C, a.TX * a.R);
   dim3 gx((n2 + a.TY - 1) / a.TY, n3, nb * C);
   dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, nb * C);
-  dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, nb);
+  dim3 gz(nb, (2 * n1 + a.TX - 1) / a.TX, 2 * n2);
   if (ev) cudaEventRecord(ev[0], stream);
   launch_x_nb<T>(n1 / 16, false, a, gx, smx, stream);
   MARIE_LAUNCH_CHECK();

@@ -20,6 +20,9 @@
 
 namespace marie {
 
+constexpr int kMaxRestart = 64;   // largest GMRES restart length
+
+
 typedef cplx<double> zd;
 constexpr int kVT = 256;          // threads per vector CTA
 constexpr int kVE = 8;            // elements per thread
@@ -321,10 +324,23 @@ __global__ void k_xupdate(const cplx<T>* V, int64_t ld, int mp1, int m, int64_t 
   const zd* y = st.y + (int64_t)r * m;
   const cplx<T>* base = V + (int64_t)r * mp1 * ld;
   zd* xr = x + (int64_t)r * xrs;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
-    zd acc = xr[i];
-    for (int j = 0; j < k; ++j) acc = acc + to_zd(base[(int64_t)j * ld + i]) * y[j];
-    xr[i] = acc;
+  if constexpr (std::is_same<T, float>::value) {
+    // complex64 basis: the combination in FP32 (the basis' own precision;
+    // FP64 arithmetic runs at 1/64 of the FP32 rate here), added to x in FP64
+    __shared__ cplx<float> yf[kMaxRestart];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) yf[j] = cplx<float>{(float)y[j].x, (float)y[j].y};
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
+      cplx<float> acc = {0, 0};
+      for (int j = 0; j < k; ++j) fma_c(acc, base[(int64_t)j * ld + i], yf[j]);
+      xr[i] = xr[i] + zd{(double)acc.x, (double)acc.y};
+    }
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
+      zd acc = xr[i];
+      for (int j = 0; j < k; ++j) acc = acc + to_zd(base[(int64_t)j * ld + i]) * y[j];
+      xr[i] = acc;
+    }
   }
 }
 
@@ -336,10 +352,21 @@ __global__ void k_rform(cplx<T>* V, int64_t ld, int mp1, int64_t Nb, const unsig
   const int k = st.kr[r];
   const zd* res = st.res + (int64_t)r * mp1;
   cplx<T>* base = V + (int64_t)r * mp1 * ld;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
-    zd acc = {0, 0};
-    for (int j = 0; j <= k; ++j) acc = acc + to_zd(base[(int64_t)j * ld + i]) * res[j];
-    base[i] = cplx<T>{(T)acc.x, (T)acc.y};
+  if constexpr (std::is_same<T, float>::value) {
+    __shared__ cplx<float> rf[kMaxRestart + 1];
+    for (int j = threadIdx.x; j <= k; j += blockDim.x) rf[j] = cplx<float>{(float)res[j].x, (float)res[j].y};
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
+      cplx<float> acc = {0, 0};
+      for (int j = 0; j <= k; ++j) fma_c(acc, base[(int64_t)j * ld + i], rf[j]);
+      base[i] = acc;
+    }
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x) {
+      zd acc = {0, 0};
+      for (int j = 0; j <= k; ++j) acc = acc + to_zd(base[(int64_t)j * ld + i]) * res[j];
+      base[i] = cplx<T>{(T)acc.x, (T)acc.y};
+    }
   }
 }
 
@@ -621,7 +648,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
                                         const marie_gmres_opts* o, marie_gmres_report* rep, void* stream) {
   if (!h || !b_ || !x_ || !o) { set_error("NULL argument"); return MARIE_ERR_BAD_ARG; }
   if (nrhs < 1) { set_error("nrhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
-  if (o->restart < 1 || o->restart > 64) { set_error("restart must be in [1, 64]"); return MARIE_ERR_BAD_ARG; }
+  if (o->restart < 1 || o->restart > kMaxRestart) { set_error("restart must be in [1, %d]", kMaxRestart); return MARIE_ERR_BAD_ARG; }
   if (o->maxit < 0) { set_error("maxit must be >= 0"); return MARIE_ERR_BAD_ARG; }
   if (!(o->tol > 0)) { set_error("tol must be > 0"); return MARIE_ERR_BAD_ARG; }
   if (o->mode != MARIE_SOLVE_FP64 && o->mode != MARIE_SOLVE_MIXED) { set_error("unknown solve mode"); return MARIE_ERR_BAD_ARG; }

@@ -180,9 +180,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   constexpr int N = 16 * NB;
   constexpr int C = PWL ? 12 : 3;
   constexpr int NE = OpTab<PWL, OP>::NE;
-  const int bu = blockIdx.z;
+  // grid (nbundle, ceil(2n1/TX), 2n2): the bundles of one (ky, kx) tile run
+  // back to back and share its Green rows in L2
+  const int bu = blockIdx.x;
   if (!bundle_active(a, bu)) return;
-  const int kyp = blockIdx.y, k0 = blockIdx.x * a.TX;
+  const int kyp = blockIdx.z, k0 = blockIdx.y * a.TX;
   const int n1 = a.n1, n2 = a.n2, m1 = 2 * n1, R = a.R;
   const int W = a.TX * R, wl = min(a.TX, m1 - k0) * R;
   const int S = kz4_stride(N, W);
