@@ -30,19 +30,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path[:0] = [str(ROOT), str(ROOT / "marie-tools_gb300")]
 
 WORKLOADS = {
-    "cfg3": dict(n=128, res=2e-3, freq=297.2e6, pwl=True, nrhs=64, tol=1e-6, phantom="ellipsoid",
+    "ellipsoid128": dict(n=128, res=2e-3, freq=297.2e6, pwl=True, nrhs=64, tol=1e-6, phantom="ellipsoid",
                  desc="ellipsoid phantom 128^3 @ 2 mm, PWL, 297.2 MHz, 64 loop-port RHS"),
-    "cfg2": dict(n=96, res=2e-3, freq=297.2e6, pwl=True, nrhs=1, tol=1e-6, phantom="ellipsoid",
+    "ellipsoid96": dict(n=96, res=2e-3, freq=297.2e6, pwl=True, nrhs=1, tol=1e-6, phantom="ellipsoid",
                  desc="ellipsoid phantom 96^3 @ 2 mm, PWL, 297.2 MHz, 1 loop RHS"),
-    "cfg1": dict(n=32, res=5e-3, freq=128e6, pwl=False, nrhs=1, tol=1e-6, phantom="sphere",
+    "sphere32": dict(n=32, res=5e-3, freq=128e6, pwl=False, nrhs=1, tol=1e-6, phantom="sphere",
                  desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
 }
 METRIC = "GMRES solves/s at 128^3 PWL, 1e-6 resid (mixed c64/FP64-refined, 64-RHS batch)"
-# Mean FP64 GMRES(50) iterations per right-hand side to 1e-6 on the cfg3
+# Mean FP64 GMRES(50) iterations per right-hand side to 1e-6 on the ellipsoid128
 # workload, measured by this library's complex128 solver (same algorithm as
 # is_gmres_vie.m); used to turn the reference arm's per-iteration time into
 # solves/s.  Updated from the 'fp64_iters_per_solve' field of our own arm.
-FP64_ITERS_CFG3 = 13.0
+FP64_ITERS_ELLIPSOID128 = 13.0
 
 
 def _dist():
@@ -255,7 +255,7 @@ def run_ours(args, wl):
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else FP64_ITERS_CFG3), budget_s=args.cpu_budget)
+        cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else FP64_ITERS_ELLIPSOID128), budget_s=args.cpu_budget)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
@@ -298,7 +298,7 @@ def run_reference(args, wl):
     ws, rank, local = _dist()
     if rank != 0:
         return
-    cpu = cpu_baseline(wl, iters=FP64_ITERS_CFG3, budget_s=1e9, steps=args.steps, warmup=args.warmup)
+    cpu = cpu_baseline(wl, iters=FP64_ITERS_ELLIPSOID128, budget_s=1e9, steps=args.steps, warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "solves/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic",
@@ -343,7 +343,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg3", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ellipsoid128", choices=sorted(WORKLOADS))
     ap.add_argument("--nrhs", type=int, default=None)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
