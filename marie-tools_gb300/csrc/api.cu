@@ -238,7 +238,6 @@ static CallTiles call_tiles(const marie_vie* h, const PrecState<T>& ps, int nr, 
   return t;
 }
 
-static bool four_step_edge(int n) { return n % 16 == 0 && n / 16 >= 1 && n / 16 <= 8; }
 
 template <typename T>
 static void fill_axis(AxisTab<T>& dst, const AxisDev<T>& src) {
@@ -367,7 +366,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   for (int c = 0; c < h->C; ++c) a.invg[c] = prec_from<T>(h->invg[c]);
   a.T1 = ps.T1;
   a.S = ps.S;
-  a.G = isK ? ps.GK : ps.GN;
+  a.G = isK ? ps.GK : ps.GN;   // octant spectra (generic path); the four-step path below uses GNf
   a.in_rs = in_rs;
   a.out_rs = out_rs;
   const int n1 = h->n1, n2 = h->n2, n3 = h->n3, C = h->C;
@@ -389,6 +388,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
     a.out = out + (int64_t)r0 * out_rs;
     a.active = active ? active + r0 : nullptr;
     if (fast) {
+      a.G = ps.GNf;
       MARIE_TRY(launch_fast_chunk<T>(h, op, a, nb, stream, (ev && r0 == 0) ? ev : nullptr));
       continue;
     }

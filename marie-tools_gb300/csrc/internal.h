@@ -55,6 +55,7 @@ struct PrecState {
   cplx<T>* chi = nullptr;     // Ns
   cplx<T>* GN = nullptr;      // nblkN * oct
   cplx<T>* GK = nullptr;      // nblkK * oct
+  cplx<T>* GNf = nullptr;     // 8 n1 n2 n3 * nblkN, [ky][kx][kz][blk] (four-step grids)
   cplx<T>* T1 = nullptr;      // ws_rhs * C * n3 * n2 * 2n1
   cplx<T>* S = nullptr;       // ws_rhs * C * 2n2 * n3 * 2n1
   int ws_rhs = 0;             // right-hand sides per matvec chunk
@@ -116,5 +117,11 @@ template <typename T>
 marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaStream_t stream, cudaEvent_t* ev);
 
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
+
+// Every grid edge is 16*NB with NB <= 8: the four-step passes apply.
+inline bool four_step_edge(int n) { return n % 16 == 0 && n / 16 >= 1 && n / 16 <= 8; }
+inline bool four_step_grid(const marie_vie* h) {
+  return four_step_edge(h->n1) && four_step_edge(h->n2) && four_step_edge(h->n3);
+}
 
 }  // namespace marie

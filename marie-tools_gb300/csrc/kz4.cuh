@@ -34,22 +34,32 @@ __device__ __forceinline__ cplx<ff> shfl_xor_c(cplx<ff> v, int m) {
 }
 
 // One entry of the single-point Green multiply (entries sorted by block;
-// every index a compile-time constant).  mx/my/mz: the point is an x/y/z
-// mirror of its octant value, each applying the block's circulant sign.
+// every index a compile-time constant).  gp points at the point's U block
+// values, contiguous in the full spectrum ([ky][kx][kz][blk], mirror signs
+// applied), so block blk sits at the constant offset blk.  complex64 loads
+// two blocks per 16-byte load.
 template <typename T, bool PWL, int OP, int K>
 struct ZPoint {
-  static __device__ __forceinline__ void run(cplx<T>* y, const cplx<T>* x, cplx<T>& gv, const cplx<T>* gp,
-                                             int64_t gblk, bool mx, bool my, bool mz) {
+  static __device__ __forceinline__ void run(cplx<T>* y, const cplx<T>* x, cplx<T>& gv, cplx<T>& gnext,
+                                             const cplx<T>* gp) {
     using Tab = OpTab<PWL, OP>;
     constexpr int blk = Tab::L.e[K].blk;
     constexpr int p = Tab::L.e[K].p, q = Tab::L.e[K].q, sg = Tab::L.e[K].sgn;
     constexpr bool first = (K == 0) || (Tab::L.e[K == 0 ? 0 : K - 1].blk != blk);
+    constexpr bool pair = sizeof(T) == 4 && (Tab::L.nblk % 2) == 0;
     if constexpr (first) {
-      constexpr bool neg1 = Tab::L.s1[blk] < 0, neg2 = Tab::L.s2[blk] < 0, neg3 = Tab::L.s3[blk] < 0;
-      cplx<T> g = ldg_c(gp + blk * gblk);
+      cplx<T> g;
+      if constexpr (pair && blk % 2 == 0) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(gp + blk));
+        g = cplx<T>{v.x, v.y};
+        gnext = cplx<T>{v.z, v.w};
+      } else if constexpr (pair) {
+        g = gnext;
+      } else {
+        g = ldg_c(gp + blk);
+      }
       if constexpr ((OP & 1) != 0) g = conjg(g);
-      const bool f = ((neg1 && mx) != (neg2 && my)) != (neg3 && mz);
-      gv = f ? cplx<T>{-g.x, -g.y} : g;
+      gv = g;
     }
     if constexpr (sg > 0) fma_c(y[p], gv, x[q]);
     else fms_c(y[p], gv, x[q]);
@@ -58,7 +68,7 @@ struct ZPoint {
 
 template <typename T, bool PWL, int OP, int... Ks>
 __device__ __forceinline__ void zpoint(std::integer_sequence<int, Ks...>, cplx<T>* v, int qstride,
-                                       const cplx<T>* gp, int64_t gblk, bool mx, bool my, bool mz) {
+                                       const cplx<T>* gp) {
   constexpr int C = PWL ? 12 : 3;
   cplx<T> x[C], y[C];
 #pragma unroll
@@ -66,8 +76,8 @@ __device__ __forceinline__ void zpoint(std::integer_sequence<int, Ks...>, cplx<T
     x[q] = v[q * qstride];
     y[q] = cplx<T>{0, 0};
   }
-  cplx<T> gv = {0, 0};
-  (ZPoint<T, PWL, OP, Ks>::run(y, x, gv, gp, gblk, mx, my, mz), ...);
+  cplx<T> gv = {0, 0}, gnext = {0, 0};
+  (ZPoint<T, PWL, OP, Ks>::run(y, x, gv, gnext, gp), ...);
 #pragma unroll
   for (int p = 0; p < C; ++p) v[p * qstride] = y[p];
 }
@@ -84,8 +94,6 @@ __device__ __forceinline__ void zpoint(std::integer_sequence<int, Ks...>, cplx<T
 struct PwlPQ {
   int jl[4][4];          // Tucker index j of entry (l, lp)
   int sg[4][4];          // its sign
-  unsigned gmask[3];     // per axis: bits k whose circulant sign is negative (j = 0)
-  unsigned bmask[3];     // per axis: bits j whose sign is negative (k = 0)
 };
 
 template <int OP>
@@ -98,14 +106,6 @@ constexpr PwlPQ make_pwl_pq() {
       t.jl[e.p][e.q] = e.blk / 6;
       t.sg[e.p][e.q] = e.sgn;
     }
-  }
-  for (int ax = 0; ax < 3; ++ax) {
-    const int* s = ax == 0 ? Tab::L.s1 : (ax == 1 ? Tab::L.s2 : Tab::L.s3);
-    unsigned g = 0, b = 0;
-    for (int k = 0; k < 6; ++k) g |= (s[k] < 0 ? 1u : 0u) << k;
-    for (int j = 0; j < 10; ++j) b |= (s[6 * j] < 0 ? 1u : 0u) << j;
-    t.gmask[ax] = g;
-    t.bmask[ax] = b;
   }
   return t;
 }
@@ -133,11 +133,8 @@ __device__ __forceinline__ void ff_cmac(cplx<ff>& y, cplx<ff> g, cplx<ff> x) {
 }
 
 template <int OP>
-__device__ __forceinline__ void zpoint_pwl_ff(cplx<ff>* v, int qstride, const cplx<ff>* gp, int64_t gblk, bool mx,
-                                              bool my, bool mz) {
+__device__ __forceinline__ void zpoint_pwl_ff(cplx<ff>* v, int qstride, const cplx<ff>* gp) {
   constexpr PwlPQ TB = make_pwl_pq<OP>();
-  const unsigned fk = (mx ? TB.gmask[0] : 0u) ^ (my ? TB.gmask[1] : 0u) ^ (mz ? TB.gmask[2] : 0u);
-  const unsigned fj = (mx ? TB.bmask[0] : 0u) ^ (my ? TB.bmask[1] : 0u) ^ (mz ? TB.bmask[2] : 0u);
   cplx<ff> y[12];
 #pragma unroll
   for (int p = 0; p < 12; ++p) y[p] = cplx<ff>{0, 0};
@@ -149,13 +146,11 @@ __device__ __forceinline__ void zpoint_pwl_ff(cplx<ff>* v, int qstride, const cp
 #pragma unroll
     for (int P = 0; P < 3; ++P) {
       const int k = P + Q + ((P > 0 && Q > 0) ? 1 : 0);    // PQ_N(P, Q) - 1
-      const cplx<ff>* gk = gp + k * gblk;
-      const unsigned fkb = (fk >> k) & 1u;
+      const cplx<ff>* gk = gp + k;                          // block (j, k) at 6j + k
 #pragma unroll
       for (int j = 0; j < 10; ++j) {
-        cplx<ff> g = ldg_c(gk + (int64_t)(6 * j) * gblk);
+        cplx<ff> g = ldg_c(gk + 6 * j);
         if constexpr ((OP & 1) != 0) g = conjg(g);
-        if ((fkb ^ (fj >> j)) & 1u) g = cplx<ff>{-g.x, -g.y};
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
 #pragma unroll
@@ -235,31 +230,24 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   __syncthreads();
 
   // Green block multiply, one frequency per item (e, g, k): kz = 2k + g sits
-  // in half g at zpos(k >> 4, k & 15).  Points above N are z-mirrors of the
-  // octant value at 2N - kz.
+  // in half g at zpos(k >> 4, k & 15); its U block values are contiguous in
+  // the full spectrum at ((ky*2n1 + kx)*2N + kz)*U.
+  constexpr int U = OpTab<PWL, OP>::L.nblk;
   const int beta = kyp / n2, ky = 2 * (kyp - beta * n2) + beta;
-  const bool my = ky > n2;
-  const int kyo = my ? 2 * n2 - ky : ky;
-  const int nko = N + 1;
-  const int64_t gblk = (int64_t)(n2 + 1) * (n1 + 1) * nko;
   for (int i = threadIdx.x; i < 2 * N * W; i += blockDim.x) {
     const int e = i % W, pp = i / W;
     const int kxp = k0 + e / R;
     if (kxp >= m1) continue;
     const int g = pp / N, k = pp - g * N;
     const int kz = 2 * k + g;
-    const bool mz = kz > N;
-    const int kzo = mz ? 2 * N - kz : kz;
     const int alpha = kxp / n1;
     const int kx = 2 * (kxp - alpha * n1) + alpha;
-    const bool mx = kx > n1;
-    const int kxo = mx ? 2 * n1 - kx : kx;
-    const cplx<T>* gp = a.G + ((int64_t)kyo * (n1 + 1) + kxo) * nko + kzo;
+    const cplx<T>* gp = a.G + (((int64_t)ky * m1 + kx) * (2 * N) + kz) * U;
     cplx<T>* v = buf + g * H + e * S + zpos(k >> 4, k & 15);
     if constexpr (PWL && std::is_same<T, ff>::value && OP <= 1)
-      zpoint_pwl_ff<OP>(v, W * S, gp, gblk, mx, my, mz);
+      zpoint_pwl_ff<OP>(v, W * S, gp);
     else
-      zpoint<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, v, W * S, gp, gblk, mx, my, mz);
+      zpoint<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, v, W * S, gp);
   }
   __syncthreads();
   // inverse step A (in place): task (s, k1), k1 fastest

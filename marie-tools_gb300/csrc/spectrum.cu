@@ -98,6 +98,29 @@ __global__ void k_oct_store(const zd* tmp, cplx<T>* dst, int nkx, int nky, int n
   }
 }
 
+// Full spectrum of one block for the four-step z pass, layout
+// [ky][kx][kz][blk] over the whole (2n2, 2n1, 2n3) grid with the circulant
+// mirror signs applied: dst[((ky*2n1 + kx)*2n3 + kz)*U + blk].
+template <typename T>
+__global__ void k_full_store(const zd* tmp, cplx<T>* dst, int n1, int n2, int n3, int U, int blk, int s1, int s2,
+                             int s3, double scl) {
+  const int m1 = 2 * n1, m2 = 2 * n2, m3 = 2 * n3;
+  const int nkx = n1 + 1, nky = n2 + 1;
+  const int64_t total = (int64_t)m1 * m2 * m3;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % m3);
+    const int64_t r = idx / m3;
+    const int kx = (int)(r % m1);
+    const int ky = (int)(r / m1);
+    const bool mx = kx > n1, my = ky > n2, mz = kz > n3;
+    const int kxo = mx ? m1 - kx : kx, kyo = my ? m2 - ky : ky, kzo = mz ? m3 - kz : kz;
+    const double sg = (double)((mx ? s1 : 1) * (my ? s2 : 1) * (mz ? s3 : 1)) * scl;
+    const zd v = tmp[kxo + (int64_t)nkx * (kyo + (int64_t)nky * kzo)];
+    dst[idx * U + blk] = cplx<T>{(T)(v.x * sg), (T)(v.y * sg)};
+  }
+}
+
 static unsigned grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 65535LL * 16) b = 65535LL * 16;
@@ -166,8 +189,18 @@ static marie_status check_parity_tucker(const marie_tucker_block& t, int n1, int
 }
 
 // Build all blocks of one operator (N or K) into the handle's spectra.
+// Spectrum destinations of one operator: octant per precision (generic
+// path, K) and full block-interleaved (four-step path, N); null = not built.
+struct SpecDst {
+  cplx<double>* o64 = nullptr;
+  cplx<float>* o32 = nullptr;
+  cplx<double>* f64 = nullptr;
+  cplx<float>* f32 = nullptr;
+  cplx<ff>* fff = nullptr;
+};
+
 static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const double* dense, int ncomp,
-                             cplx<double>* dst64, cplx<float>* dst32, cplx<ff>* dstff) {
+                             const SpecDst& dst) {
   const int n1 = h->n1, n2 = h->n2, n3 = h->n3;
   const int pwx = h->pwl ? 10 : 1;
   const int nblk = pwx * ncomp;
@@ -197,6 +230,24 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
   marie_status st = MARIE_OK;
   const int tabk = ncomp == 6 ? 0 : 2;   // N or K table (mirror signs)
   const BlockTab& bt = h->tab[tabk];
+  const int64_t full = (int64_t)8 * n1 * n2 * n3;
+  auto store_block = [&](int id) {
+    if (dst.o64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst.o64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+    if (dst.o32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst.o32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
+    const int s1 = bt.s1[id], s2 = bt.s2[id], s3 = bt.s3[id];
+    if (dst.f64) {
+      k_full_store<double><<<grid_for(full), 256>>>(tmp, dst.f64, n1, n2, n3, nblk, id, s1, s2, s3, scl);
+      g_launches++;
+    }
+    if (dst.f32) {
+      k_full_store<float><<<grid_for(full), 256>>>(tmp, dst.f32, n1, n2, n3, nblk, id, s1, s2, s3, scl);
+      g_launches++;
+    }
+    if (dst.fff) {
+      k_full_store<ff><<<grid_for(full), 256>>>(tmp, dst.fff, n1, n2, n3, nblk, id, s1, s2, s3, scl);
+      g_launches++;
+    }
+  };
   do {
     if ((st = salloc(&tmp, oct)) != MARIE_OK) break;
     if (dense) {
@@ -235,9 +286,7 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
         g_launches++;
         k_circ_axis<<<grid_for(oct), 256>>>(c, tmp, n3, bt.s3[id], (int64_t)nkx * nky, 1, w3);
         g_launches++;
-        if (dst64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
-        if (dst32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
-        if (dstff) { k_oct_store<ff><<<grid_for(oct), 256>>>(tmp, dstff + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        store_block(id);
         if (cudaGetLastError() != cudaSuccess) { set_error("spectrum kernel launch failed"); st = MARIE_ERR_CUDA; break; }
         cudaDeviceSynchronize();
       }
@@ -277,9 +326,7 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
         g_launches++;
         k_tk3<<<grid_for(oct), 256>>>(b, dU1, tmp, t.r1, nkx, nky, nkz);
         g_launches++;
-        if (dst64) { k_oct_store<double><<<grid_for(oct), 256>>>(tmp, dst64 + id * oct, nkx, nky, nkz, scl); g_launches++; }
-        if (dst32) { k_oct_store<float><<<grid_for(oct), 256>>>(tmp, dst32 + id * oct, nkx, nky, nkz, scl); g_launches++; }
-        if (dstff) { k_oct_store<ff><<<grid_for(oct), 256>>>(tmp, dstff + id * oct, nkx, nky, nkz, scl); g_launches++; }
+        store_block(id);
         if (cudaGetLastError() != cudaSuccess) { set_error("spectrum kernel launch failed"); st = MARIE_ERR_CUDA; break; }
         cudaDeviceSynchronize();
       }
@@ -291,21 +338,33 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
 
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d) {
   const int64_t oct = (int64_t)(h->n1 + 1) * (h->n2 + 1) * (h->n3 + 1);
+  const int64_t full = (int64_t)8 * h->n1 * h->n2 * h->n3;
+  const bool fast = four_step_grid(h);
   if (h->precisions & 1) {
     MARIE_TRY(dev_alloc(h, (void**)&h->p64.GN, (size_t)h->nblkN * oct * sizeof(cplx<double>)));
     if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->p64.GK, (size_t)h->nblkK * oct * sizeof(cplx<double>)));
+    if (fast) MARIE_TRY(dev_alloc(h, (void**)&h->p64.GNf, (size_t)h->nblkN * full * sizeof(cplx<double>)));
   }
   if (h->precisions & 2) {
     MARIE_TRY(dev_alloc(h, (void**)&h->p32.GN, (size_t)h->nblkN * oct * sizeof(cplx<float>)));
     if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->p32.GK, (size_t)h->nblkK * oct * sizeof(cplx<float>)));
+    if (fast) MARIE_TRY(dev_alloc(h, (void**)&h->p32.GNf, (size_t)h->nblkN * full * sizeof(cplx<float>)));
   }
-  if (h->precisions & 4) {
-    MARIE_TRY(dev_alloc(h, (void**)&h->pff.GN, (size_t)h->nblkN * oct * sizeof(cplx<ff>)));
-    if (h->has_K) MARIE_TRY(dev_alloc(h, (void**)&h->pff.GK, (size_t)h->nblkK * oct * sizeof(cplx<ff>)));
+  if (h->precisions & 4)   // float-float: four-step path only (N and N^H)
+    MARIE_TRY(dev_alloc(h, (void**)&h->pff.GNf, (size_t)h->nblkN * full * sizeof(cplx<ff>)));
+  SpecDst dN;
+  dN.o64 = h->p64.GN;
+  dN.o32 = h->p32.GN;
+  dN.f64 = h->p64.GNf;
+  dN.f32 = h->p32.GNf;
+  dN.fff = h->pff.GNf;
+  MARIE_TRY(build_op(h, d->tucker_N, d->tucker_N ? nullptr : d->dense_N, 6, dN));
+  if (h->has_K) {
+    SpecDst dK;
+    dK.o64 = h->p64.GK;
+    dK.o32 = h->p32.GK;
+    MARIE_TRY(build_op(h, d->tucker_K, d->tucker_K ? nullptr : d->dense_K, 3, dK));
   }
-  MARIE_TRY(build_op(h, d->tucker_N, d->tucker_N ? nullptr : d->dense_N, 6, h->p64.GN, h->p32.GN, h->pff.GN));
-  if (h->has_K)
-    MARIE_TRY(build_op(h, d->tucker_K, d->tucker_K ? nullptr : d->dense_K, 3, h->p64.GK, h->p32.GK, h->pff.GK));
   return MARIE_OK;
 }
 
