@@ -169,6 +169,25 @@ marie_status marie_incident_loops(marie_vie* h, const double* origin, const doub
 /* Unit x-polarised plane wave exp(-i k0 z) tested onto the basis. */
 marie_status marie_incident_plane_wave(marie_vie* h, const double* origin, void* out_dev, void* stream);
 
+/* Field post-processing of solved body currents J (device, nrhs x N_b, the
+ * handle's body-vector layout) in precision prec.
+ * E = Ue + mask.*invG((1/ce)(N J - G J))  (em_efield_vie_excitation.m:21)
+ * H = Ub + mask.*invG(K J)                (em_hfield_vie_excitation.m:20)
+ * restricted to the body; Ue / Ub (incident fields, same layout) may be NULL
+ * (zero); E or H may be NULL (not computed).  H needs the K operator. */
+marie_status marie_vie_fields(marie_vie* h, int32_t prec, const void* J, const void* Ue, const void* Ub, void* E,
+                              void* H, int32_t nrhs, void* stream);
+/* Absorbed-power / noise-covariance matrix of em_ehfield_vie.m:44-52:
+ * phi = conj(J^H (real(Mpow) .* (G J))), Mpow = Mc_inv/ce per body voxel
+ * (0 where Mc = 0).  J: device complex128, nrhs x N_b (nrhs <= 64);
+ * phi_host: host, nrhs x nrhs complex128 (row p, column q), FP64 sums in a
+ * fixed order. */
+marie_status marie_vie_absorbed_power(marie_vie* h, const void* J, int32_t nrhs, double* phi_host, void* stream);
+/* B1+ = mu0 (H_x + i H_y) on the constant moment of each body voxel
+ * (em_ehfield_vie.m:68).  H: device complex128, nrhs x N_b; out: device
+ * complex128, nrhs x N_s. */
+marie_status marie_vie_b1_plus(marie_vie* h, const void* H, int32_t nrhs, void* out, void* stream);
+
 /* Diagnostics. */
 /* Average device time [ms] of each matvec pass over `reps` repetitions of
  * one mvp_vie application of nrhs right-hand sides (x/y: device, precision

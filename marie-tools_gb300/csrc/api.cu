@@ -7,6 +7,7 @@
 #include <mutex>
 #include <new>
 
+#include "fastpath.cuh"
 #include "internal.h"
 
 namespace marie {
@@ -203,12 +204,25 @@ static void make_tables(marie_vie* h) {
 // Z-pass tile width W = TX*R (contiguous elements per (component, z) row):
 // the largest power of two whose shared-memory tile fits ~100 KB (two CTAs per
 // SM).  The bundle size R is at most W.
+static int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  if (!v || !*v) return dflt;
+  return atoi(v);
+}
+
 template <typename T>
 static void choose_tiles(marie_vie* h, PrecState<T>& ps) {
   const int n3 = h->n3, C = h->C;
   const int sz = (int)sizeof(cplx<T>);
   int W = 16;
   while (W > 1 && (size_t)n3 * (2 * C * W + 1) * sz > 100 * 1024) W /= 2;
+  // MARIE_Z_TILE: z-pass tile width (power of two <= 16) if its shared
+  // memory fits one CTA (227 KB)
+  const int wz = env_int("MARIE_Z_TILE", 0);
+  const size_t lim = 227 * 1024;
+  if (wz >= 1 && wz <= 16 && (wz & (wz - 1)) == 0 && (size_t)n3 * (2 * C * wz + 2) * sz <= lim &&
+      kz4_smem<T>(n3, C, wz) <= lim)
+    W = wz;
   ps.TX = W;      // Wz
   ps.TY = 0;
   ps.TXY = 0;
@@ -248,11 +262,6 @@ static void fill_axis(AxisTab<T>& dst, const AxisDev<T>& src) {
   dst.plan = src.plan;
 }
 
-static int env_int(const char* name, int dflt) {
-  const char* v = getenv(name);
-  if (!v || !*v) return dflt;
-  return atoi(v);
-}
 
 template <typename T>
 static marie_status alloc_workspace(marie_vie* h, PrecState<T>& ps) {
@@ -275,7 +284,8 @@ static void set_smem_attr(const void* fn) {
 template <typename T>
 static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<typename IoOf<T>::type>* in,
                                      int64_t in_rs, cplx<typename IoOf<T>::type>* out, int64_t out_rs, int nrhs,
-                                     const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev);
+                                     const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev,
+                                     const cplx<typename IoOf<T>::type>* addend = nullptr);
 
 template <typename T, bool PWL, int OP>
 static void launch_z(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
@@ -322,7 +332,8 @@ marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, in
 template <typename T>
 static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<typename IoOf<T>::type>* in,
                                      int64_t in_rs, cplx<typename IoOf<T>::type>* out, int64_t out_rs, int nrhs,
-                                     const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev) {
+                                     const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev,
+                                     const cplx<typename IoOf<T>::type>* addend) {
   PrecState<T>& ps = prec_state<T>(h);
   if (!ps.built) {
     set_error("precision not built for this handle");
@@ -364,6 +375,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   }
   a.chi = ps.chi;
   for (int c = 0; c < h->C; ++c) a.invg[c] = prec_from<T>(h->invg[c]);
+  a.efac = cplx<T>{prec_from<T>(0.0L), prec_from<T>(-1.0L / (long double)h->ce_im)};   // 1/ce, ce = i*omega*eps0
   a.T1 = ps.T1;
   a.S = ps.S;
   a.G = isK ? ps.GK : ps.GN;   // octant spectra (generic path); the four-step path below uses GNf
@@ -387,6 +399,7 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
     a.in = in + (int64_t)r0 * in_rs;
     a.out = out + (int64_t)r0 * out_rs;
     a.active = active ? active + r0 : nullptr;
+    a.addend = addend ? addend + (int64_t)r0 * out_rs : nullptr;
     if (fast) {
       a.G = ps.GNf;
       MARIE_TRY(launch_fast_chunk<T>(h, op, a, nb, stream, (ev && r0 == 0) ? ev : nullptr));
@@ -424,6 +437,20 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   }
   return MARIE_OK;
 }
+
+template <typename T>
+marie_status launch_matvec_fields(marie_vie* h, int mode, int op, const cplx<T>* in, cplx<T>* out,
+                                  const cplx<T>* addend, int nrhs, cudaStream_t stream) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (c128_is_ff(h))
+      return launch_matvec_ev<ff>(h, mode, op, in, h->Nb, out, h->Nb, nrhs, nullptr, stream, nullptr, addend);
+  }
+  return launch_matvec_ev<T>(h, mode, op, in, h->Nb, out, h->Nb, nrhs, nullptr, stream, nullptr, addend);
+}
+template marie_status launch_matvec_fields<float>(marie_vie*, int, int, const cplx<float>*, cplx<float>*,
+                                                  const cplx<float>*, int, cudaStream_t);
+template marie_status launch_matvec_fields<double>(marie_vie*, int, int, const cplx<double>*, cplx<double>*,
+                                                   const cplx<double>*, int, cudaStream_t);
 
 template marie_status launch_matvec<float>(marie_vie*, int, int, const cplx<float>*, int64_t, cplx<float>*, int64_t,
                                            int, const unsigned char*, cudaStream_t);
@@ -494,6 +521,7 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   const double mu0 = 4e-7 * M_PI, c0 = 299792458.0;
   const double e0 = 1.0 / (c0 * c0 * mu0);
   h->omega = 2 * M_PI * d->freq;
+  h->ce_im = h->omega * e0;    // ce = i*omega*eps0 (em_constants.m)
   h->k0 = 2 * M_PI / (c0 / d->freq);
   h->Nb = d->n_b;
   h->Ns = d->n_b / h->C;
@@ -565,6 +593,7 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   cudaMemcpy(h->idxS, idxS.data(), h->Ns * sizeof(int64_t), cudaMemcpyHostToDevice);
   // contrast chi = (1./Mr).*Mc on the body (mvp_vie.m:17)
   std::vector<cplx<double>> chi(h->Ns);
+  std::vector<double> wpow(h->Ns);
   for (int64_t s = 0; s < h->Ns; ++s) {
     const std::complex<double> Mr(d->Mr[2 * idxS[s]], d->Mr[2 * idxS[s] + 1]);
     if (!std::isfinite(Mr.real()) || !std::isfinite(Mr.imag()) || Mr == 0.0) {
@@ -574,7 +603,11 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
     const std::complex<double> Mc = Mr - 1.0;
     const std::complex<double> v = (1.0 / Mr) * Mc;
     chi[s] = cplx<double>{v.real(), v.imag()};
+    // real(Mc_inv / ce), the absorbed-power weight of em_ehfield_vie.m:46 (0 where Mc = 0)
+    wpow[s] = Mc == 0.0 ? 0.0 : ((1.0 / Mc) / std::complex<double>(0.0, h->ce_im)).real();
   }
+  if ((st = dev_alloc(h, (void**)&h->wpow, h->Ns * sizeof(double))) != MARIE_OK) return fail(st);
+  cudaMemcpy(h->wpow, wpow.data(), h->Ns * sizeof(double), cudaMemcpyHostToDevice);
   (void)e0;
   for (int pr = 0; pr < 3; ++pr) {
     if (!(d->precisions & (1 << pr))) continue;

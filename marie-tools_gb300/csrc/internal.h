@@ -67,6 +67,7 @@ struct PrecState {
 struct marie_vie {
   int n1 = 0, n2 = 0, n3 = 0, C = 0, pwl = 0;
   double res = 0, freq = 0, k0 = 0, omega = 0;
+  double ce_im = 0;                  // ce = i*ce_im = i*omega*eps0
   int64_t Ns = 0, Nb = 0;
   int device = 0;
   int max_rhs = 1;
@@ -81,6 +82,7 @@ struct marie_vie {
   uint16_t* rowq = nullptr;          // device, n3*8: row_live in four-step order (n2 = 16*NB)
   uint16_t* zq = nullptr;            // device, 8: z_live in four-step order (n3 = 16*NB)
   int64_t* idxS = nullptr;           // device, Ns (0-based linear voxel index)
+  double* wpow = nullptr;            // device, Ns: real(Mc_inv/ce) per body voxel
   std::vector<int64_t> idxS_host;
   marie::BlockTab tab[4];            // N, N_adj, K, K_adj
   marie::PrecState<double> p64;
@@ -110,6 +112,12 @@ marie_status launch_matvec(marie_vie* h, int mode, int op, const cplx<T>* in, in
 
 template <typename T>
 PrecState<T>& prec_state(marie_vie* h);
+
+// Field modes (MV_EFIELD / MV_HFIELD) on body vectors of length N_b, with an
+// optional addend (incident field) of the same layout.
+template <typename T>
+marie_status launch_matvec_fields(marie_vie* h, int mode, int op, const cplx<T>* in, cplx<T>* out,
+                                  const cplx<T>* addend, int nrhs, cudaStream_t stream);
 
 // Four-step passes (grid edges 16*NB, NB <= 8) for one chunk of nb bundles;
 // tiles and bundle size are set in `a` by the caller.

@@ -39,6 +39,8 @@ enum MvMode : int {
   MV_GRID = 0,      // input/output are full grids (n1,n2,n3,C) column-major
   MV_VIE = 1,       // y = x - chi .* invG(N x) on the body vector
   MV_VIE_ADJ = 2,   // y = x - N^H(invG .* conj(chi) .* x) on the body vector
+  MV_EFIELD = 3,    // y = (1/ce) (invG(N x) - x) on the body (em_efield_vie_excitation.m:21)
+  MV_HFIELD = 4,    // y = invG(K x) on the body (em_hfield_vie_excitation.m:20)
 };
 
 // Per-axis lookup tables (device pointers).
@@ -79,6 +81,8 @@ struct MvArgs {
   cplx<T>* S;                 // [bundle][c][2n2][z][2n1][R]
   const cplx<T>* G;           // octant spectra [blk][n2+1][n1+1][n3+1]
   const unsigned char* active;  // per rhs: nonzero = process (may be null)
+  cplx<T> efac;               // 1/ce (MV_EFIELD)
+  const cplx<typename IoOf<T>::type>* addend;   // added to the body output (same strides; may be null)
   // Body occupancy for the pruned four-step passes (null: every row live).
   // row_live[z*n2 + y]: the grid row (y, z) holds a body voxel; z_live[z]:
   // slice z does.  Rows and slices that are not live are zero on input and
@@ -111,6 +115,24 @@ __device__ __forceinline__ bool row_is_live(const MvArgs<T>& a, int y, int z) {
 template <typename T>
 __device__ __forceinline__ bool z_is_live(const MvArgs<T>& a, int z) {
   return a.z_live == nullptr || a.z_live[z] != 0;
+}
+
+// Body-vector output of the modes other than MV_GRID for component c, body
+// voxel s and right-hand side rhs, given v = (operator x) at that voxel.
+template <typename T>
+__device__ __forceinline__ void body_store(const MvArgs<T>& a, int c, int s, int rhs, cplx<T> v) {
+  const int64_t o = (int64_t)c * a.Ns + s;
+  cplx<T> r;
+  if (a.mode == MV_HFIELD) {
+    r = scale(v, a.invg[c]);
+  } else {
+    const cplx<T> xin = io_load<T>(a.in[(int64_t)rhs * a.in_rs + o]);
+    if (a.mode == MV_VIE) r = xin - scale(a.chi[s] * v, a.invg[c]);
+    else if (a.mode == MV_VIE_ADJ) r = xin - v;
+    else r = a.efac * (scale(v, a.invg[c]) - xin);
+  }
+  if (a.addend) r = r + io_load<T>(a.addend[(int64_t)rhs * a.out_rs + o]);
+  a.out[(int64_t)rhs * a.out_rs + o] = io_store(r);
 }
 
 template <typename T>
@@ -289,7 +311,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_z(MvArgs<T> a) 
   const int kyp = blockIdx.y, k0 = blockIdx.x * a.TX;
   const int n1 = a.n1, n2 = a.n2, n3 = a.n3, m1 = 2 * n1, TX = a.TX, R = a.R;
   constexpr int C = PWL ? 12 : 3;
-  constexpr int NE = OpTab<PWL, OP>::NE;
   const int tx = min(TX, m1 - k0);
   const int W = TX * R;                    // contiguous elements per (c, z)
   const int nseq = 2 * C * W, es = nseq + 1;
@@ -430,12 +451,7 @@ __global__ void k_inv_x(MvArgs<T> a) {
       a.out[(int64_t)rhs * a.out_rs + (int64_t)c * nD + g] = v;
     } else {
       const int s = a.vox2sol[g];
-      if (s >= 0) {
-        const int64_t o = (int64_t)c * a.Ns + s;
-        const cplx<T> xin = a.in[(int64_t)rhs * a.in_rs + o];
-        if (a.mode == MV_VIE) v = scale(a.chi[s] * v, a.invg[c]);
-        a.out[(int64_t)rhs * a.out_rs + o] = xin - v;
-      }
+      if (s >= 0) body_store(a, c, s, rhs, v);
     }
   }
 }

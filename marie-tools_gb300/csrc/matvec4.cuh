@@ -228,12 +228,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_x(MvArgs<T
         a.out[(int64_t)rhs * a.out_rs + (int64_t)c * nD + grow + x] = io_store(v);
       } else {
         const int s = a.vox2sol[grow + x];
-        if (s >= 0) {
-          const int64_t o = (int64_t)c * a.Ns + s;
-          const cplx<T> xin = io_load<T>(a.in[(int64_t)rhs * a.in_rs + o]);
-          if (a.mode == MV_VIE) v = scale(a.chi[s] * v, a.invg[c]);
-          a.out[(int64_t)rhs * a.out_rs + o] = io_store(xin - v);
-        }
+        if (s >= 0) body_store(a, c, s, rhs, v);
       }
     }
   }

@@ -80,6 +80,9 @@ _PROTOS = {
                                              _vp]),
     "marie_vie_profile": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, ct.c_int32, c_double_p, _vp]),
     "marie_vie_tiles": (ct.c_int, [_vp, ct.c_int32, c_int32_p]),
+    "marie_vie_fields": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, _vp, _vp, _vp, ct.c_int32, _vp]),
+    "marie_vie_absorbed_power": (ct.c_int, [_vp, _vp, ct.c_int32, c_double_p, _vp]),
+    "marie_vie_b1_plus": (ct.c_int, [_vp, _vp, ct.c_int32, _vp, _vp]),
     "marie_last_error": (ct.c_char_p, []),
     "marie_version": (ct.c_char_p, []),
     "marie_launch_count": (ct.c_int64, []),

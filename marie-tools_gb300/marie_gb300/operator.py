@@ -178,6 +178,52 @@ class VieOperator:
         check(self._lib.marie_vie_tiles(self._h, prec, out.ctypes.data_as(_lib.c_int32_p)))
         return dict(chunk=int(out[0]), width=int(out[1]), float_float=bool(out[2]))
 
+    # -- field post-processing -------------------------------------------------
+    def fields(self, J, Ue=None, Ub=None, *, e=True, h=True):
+        """Total fields of solved body currents J (nrhs*N_b, complex64/128 CUDA):
+        E = Ue + invG((1/ce)(N J - G J)) (em_efield_vie_excitation.m:21) and
+        H = Ub + invG(K J) (em_hfield_vie_excitation.m:20) on the body."""
+        import torch
+        if J.device.type != "cuda" or J.dtype not in (torch.complex64, torch.complex128):
+            raise ValueError("J must be a complex64 or complex128 CUDA tensor")
+        J = J.contiguous()
+        prec = C128 if J.dtype == torch.complex128 else C64
+        nrhs = J.numel() // self.Nb
+        ptr = lambda t: ct.c_void_p(t.data_ptr()) if t is not None else None
+        for t in (Ue, Ub):
+            if t is not None and (t.dtype != J.dtype or t.numel() != J.numel() or not t.is_contiguous()):
+                raise ValueError("Ue/Ub must match J in dtype and length and be contiguous")
+        E = torch.empty_like(J) if e else None
+        H = torch.empty_like(J) if h else None
+        check(self._lib.marie_vie_fields(self._h, prec, ptr(J), ptr(Ue), ptr(Ub), ptr(E), ptr(H), nrhs,
+                                         self._stream()))
+        return E, H
+
+    def absorbed_power(self, J):
+        """phi = conj(J^H (real(Mc_inv/ce) .* G J)) (em_ehfield_vie.m:44-52); J: complex128 CUDA,
+        nrhs*N_b with nrhs <= 64; returns an (nrhs, nrhs) complex128 numpy array."""
+        import torch
+        if J.device.type != "cuda" or J.dtype != torch.complex128:
+            raise ValueError("J must be a complex128 CUDA tensor")
+        J = J.contiguous()
+        nrhs = J.numel() // self.Nb
+        phi = np.zeros(2 * nrhs * nrhs, np.float64)
+        check(self._lib.marie_vie_absorbed_power(self._h, ct.c_void_p(J.data_ptr()), nrhs, _dptr(phi),
+                                                 self._stream()))
+        return phi.view(np.complex128).reshape(nrhs, nrhs)
+
+    def b1_plus(self, H):
+        """B1+ = mu0 (H_x + i H_y) per body voxel (em_ehfield_vie.m:68); H: complex128 CUDA nrhs*N_b."""
+        import torch
+        if H.device.type != "cuda" or H.dtype != torch.complex128:
+            raise ValueError("H must be a complex128 CUDA tensor")
+        H = H.contiguous()
+        nrhs = H.numel() // self.Nb
+        out = torch.empty(nrhs * self.Ns, dtype=torch.complex128, device="cuda")
+        check(self._lib.marie_vie_b1_plus(self._h, ct.c_void_p(H.data_ptr()), nrhs, ct.c_void_p(out.data_ptr()),
+                                          self._stream()))
+        return out
+
     # -- solve ----------------------------------------------------------------
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
               max_refine=10, resvec_cap=4096, raise_on_fail=False):

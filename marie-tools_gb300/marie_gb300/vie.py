@@ -162,3 +162,43 @@ def ie_solver_vie(fN: VieOperator, Ue, ce, Mr, Mc, idxS, tol, restart=50, maxit=
     U = _to_cuda(Ue, torch.complex128).reshape(fN.Nb, -1)
     rhs = ce * _to_cuda(chi, torch.complex128)[:, None] * U
     return is_gmres_vie(fN, rhs, restart, tol, maxit, None, mode=mode)
+
+
+def _ports(a, op, dtype):
+    """(N_b, N_ports) array (MATLAB layout) -> contiguous (N_ports*N_b) CUDA vector."""
+    import torch
+    A = _to_cuda(a, dtype).reshape(op.Nb, -1)
+    return A.t().contiguous().reshape(-1), A.shape[1]
+
+
+def em_efield_vie_excitation(op: VieOperator, Jb, Ue):
+    """em_efield_vie_excitation.m:17-23 for every port at once:
+    Ue + mask.*invG((1/ce)(mvp_N(Jb) - mvp_G(Jb))) on the body.  Jb, Ue:
+    (N_b, N_ports); returns (N_b, N_ports) complex128 on the GPU."""
+    import torch
+    J, npt = _ports(Jb, op, torch.complex128)
+    U, _ = _ports(Ue, op, torch.complex128)
+    E, _h = op.fields(J, Ue=U, e=True, h=False)
+    return E.reshape(npt, op.Nb).t()
+
+
+def em_hfield_vie_excitation(op: VieOperator, Jb, Ub):
+    """em_hfield_vie_excitation.m:16-22: Ub + mask.*invG(mvp_K(Jb)) on the body."""
+    import torch
+    J, npt = _ports(Jb, op, torch.complex128)
+    U, _ = _ports(Ub, op, torch.complex128)
+    _e, H = op.fields(J, Ub=U, e=False, h=True)
+    return H.reshape(npt, op.Nb).t()
+
+
+def em_ehfield_vie(op: VieOperator, Jb, Ue, Ub):
+    """Field part of em_ehfield_vie.m:31-52: total E and H fields per port and
+    the noise-covariance matrix phi; the ultimate-SNR/TXE metrics that follow
+    (em_ehfield_vie.m:54-) are outside this library."""
+    import torch
+    J, npt = _ports(Jb, op, torch.complex128)
+    Ut, _ = _ports(Ue, op, torch.complex128)
+    Bt, _ = _ports(Ub, op, torch.complex128)
+    E, H = op.fields(J, Ue=Ut, Ub=Bt)
+    phi = op.absorbed_power(J)
+    return E.reshape(npt, op.Nb).t(), H.reshape(npt, op.Nb).t(), phi

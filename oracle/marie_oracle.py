@@ -443,6 +443,49 @@ def mvp_vie_adjoint(Jb, Mr, Mc, dims, T, cache=None):
 
 
 # ---------------------------------------------------------------------------
+# Field post-processing
+# ---------------------------------------------------------------------------
+
+
+def em_efield_vie_excitation(Jb, Ue, dims, T_N, ce, cache=None):
+    """Restates em_efield_vie_excitation.m:17-23 for one port:
+    Ue + mask.*invG((1/ce)(mvp_N(Jb) - mvp_G(Jb))) on the body."""
+    Jp = scatter(Jb, dims)
+    pwl = dims["ql"] == 12
+    NJ = mvp_op_tucker(Jp, T_N, "N", False, cache)
+    GJ = G_scale(pwl, dims["res"])[None, None, None, :] * Jp
+    e = invG_scale(pwl, dims["res"])[None, None, None, :] * ((NJ - GJ) / ce)
+    return Ue + gather(e, dims)
+
+
+def em_hfield_vie_excitation(Jb, Ub, dims, T_K, cache=None):
+    """Restates em_hfield_vie_excitation.m:16-22 for one port:
+    Ub + mask.*invG(mvp_K(Jb)) on the body."""
+    Jp = scatter(Jb, dims)
+    pwl = dims["ql"] == 12
+    KJ = mvp_op_tucker(Jp, T_K, "K", False, cache)
+    return Ub + gather(invG_scale(pwl, dims["res"])[None, None, None, :] * KJ, dims)
+
+
+def em_noise_covariance(J, Mc, ce, dims):
+    """Restates em_ehfield_vie.m:44-52: Mpow = repmat(Mc_inv(idxS),[ql 1])/ce,
+    Gx = mvp_G(J) on the body, phi = conj(J' * (real(Mpow) .* Gx)).
+    J: (N_b, N_ports)."""
+    pwl = dims["ql"] == 12
+    mc = np.asarray(Mc).reshape(-1, order="F")[dims["idxS"]]
+    mpow = np.tile(1.0 / mc, dims["ql"]) / ce
+    g = np.repeat(G_scale(pwl, dims["res"]), dims["N_scat"])
+    Gx = g[:, None] * J
+    return np.conj(J.conj().T @ (np.real(mpow)[:, None] * Gx))
+
+
+def b1_plus(Ub, dims, mu0):
+    """B1+ = mu0 (Ub(jj) + 1i Ub(jj + N_scat*l)) per body voxel (em_ehfield_vie.m:68)."""
+    ns, l = dims["N_scat"], dims["l"]
+    return mu0 * (Ub[:ns] + 1j * Ub[l * ns:l * ns + ns])
+
+
+# ---------------------------------------------------------------------------
 # GMRES
 # ---------------------------------------------------------------------------
 

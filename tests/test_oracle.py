@@ -181,3 +181,21 @@ def test_gmres_restart_bookkeeping():
     true = np.linalg.norm(b - A(x)) / np.linalg.norm(b)
     assert rv[-1] <= 1e-8
     assert abs(true - rv[-1]) < 1e-9
+
+
+def test_field_postprocessing_oracle_identities():
+    """E/H post-processing and the noise covariance of the oracle: zero
+    currents return the incident fields, the fields are linear in J, and phi
+    is Hermitian (em_ehfield_vie.m:44-52)."""
+    P = Problem((6, 5, 4), True, seed=4)
+    rng = np.random.default_rng(0)
+    Nb = P.dims["N_b"]
+    J1, J2, U = (rng.normal(size=Nb) + 1j * rng.normal(size=Nb) for _ in range(3))
+    ce = P.emc["ce"]
+    assert np.allclose(O.em_efield_vie_excitation(0 * J1, U, P.dims, P.TN, ce), U)
+    e = lambda J: O.em_efield_vie_excitation(J, 0 * U, P.dims, P.TN, ce)
+    h = lambda J: O.em_hfield_vie_excitation(J, 0 * U, P.dims, P.TK)
+    assert rel_err(e(J1 + 2 * J2), e(J1) + 2 * e(J2)) < 1e-13
+    assert rel_err(h(J1 - 3j * J2), h(J1) - 3j * h(J2)) < 1e-13
+    phi = O.em_noise_covariance(np.stack([J1, J2, U], 1), P.Mc, ce, P.dims)
+    assert np.allclose(phi, phi.conj().T, rtol=1e-13, atol=0)
