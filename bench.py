@@ -205,17 +205,18 @@ def run_ours(args, wl):
     ms_max = float(t.item())
     value = nrhs * args.steps * ws / (ms_max * 1e-3)
 
-    # end to end through the public API: pinned host b -> device, solve, x -> host
+    # end to end through the public API on host buffers (marie_gmres_vie_host:
+    # pinned b in, x out, copies inside the timed region, overlapped with the
+    # chunked solve)
     b_host = b.cpu().pin_memory()
     x_host = torch.empty_like(b_host).pin_memory()
+    op.gmres_host(b_host, out=x_host, **kw)      # warm-up of the host path's device buffers
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e2.record(stream)
     nE = max(1, min(args.steps, 2))
     for _ in range(nE):
-        bd = b_host.to("cuda", non_blocking=True)
-        xd, _r = op.gmres(bd, **kw)
-        x_host.copy_(xd, non_blocking=True)
+        op.gmres_host(b_host, out=x_host, **kw)
     e3.record(stream)
     torch.cuda.synchronize()
     ms_e2e = e2.elapsed_time(e3) / nE

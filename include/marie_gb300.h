@@ -154,6 +154,20 @@ typedef struct {
 marie_status marie_gmres_vie(marie_vie* h, const void* b, void* x, int32_t nrhs,
                              const marie_gmres_opts* opts, marie_gmres_report* report, void* stream);
 
+/* marie_gmres_vie with b and x in host memory (nrhs x N_b complex128; x
+ * holds x0 on entry when opts->x0_present).  The right-hand sides are solved
+ * in chunks of the matvec chunk size; copies of the next chunk in and the
+ * previous chunk out run on a second stream while a chunk is solved, so with
+ * page-locked host buffers only the first copy in and the last copy out are
+ * exposed.  The MATLAB host-array path of is_gmres_vie (to_GPU.m:8-51). */
+marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, void* x_host, int32_t nrhs,
+                                  const marie_gmres_opts* opts, marie_gmres_report* report, void* stream);
+
+/* Frees the GMRES workspace the handle keeps between solves (Krylov basis,
+ * residual vectors; reused by the next solve of the same or smaller shape).
+ * No counterpart in the reference (MATLAB frees its arrays itself). */
+marie_status marie_vie_release_workspace(marie_vie* h);
+
 /* Operator-generation helpers (producers of the hot path's operands). */
 /* I_V of assembly_N.m / assembly_K.m (far and medium zones by 6D Gauss rules,
  * near zone {0,1}^3 by the staggered stand-in rule); out: host, dense

@@ -47,6 +47,10 @@ marie_status dev_alloc(marie_vie* h, void** p, size_t bytes) {
 void dev_free_all(marie_vie* h) {
   for (void* p : h->allocs) cudaFree(p);
   h->allocs.clear();
+  for (auto& e : h->gm_pool) cudaFree(e.first);
+  h->gm_pool.clear();
+  for (auto& e : h->io_pool) cudaFree(e.first);
+  h->io_pool.clear();
   h->mem_used = 0;
 }
 
@@ -653,6 +657,19 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
     return fail(MARIE_ERR_CUDA);
   }
   *out = h;
+  return MARIE_OK;
+}
+
+marie_status marie_vie_release_workspace(marie_vie* h) {
+  if (!h) { set_error("handle is NULL"); return MARIE_ERR_BAD_ARG; }
+  cudaDeviceSynchronize();
+  for (auto* pool : {&h->gm_pool, &h->io_pool}) {
+    for (auto& e : *pool) {
+      cudaFree(e.first);
+      h->mem_used -= (int64_t)e.second;
+    }
+    pool->clear();
+  }
   return MARIE_OK;
 }
 

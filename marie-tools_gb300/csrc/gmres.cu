@@ -412,27 +412,44 @@ __global__ void k_zero(zd* x, int64_t n) {
 // Host side
 // ---------------------------------------------------------------------------
 
+// Workspace of one solve, served from the handle's pool: the k-th request
+// of a solve reuses the pool's k-th buffer when it is large enough (solves
+// with the same shape request the same sequence), else replaces it.
 struct Scratch {
-  std::vector<void*> ptrs;
   marie_vie* h;
-  explicit Scratch(marie_vie* hh) : h(hh) {}
-  ~Scratch() {
-    for (void* p : ptrs) cudaFree(p);
-  }
+  std::vector<std::pair<void*, size_t>>* pool;
+  size_t next = 0;
+  explicit Scratch(marie_vie* hh) : h(hh), pool(&hh->gm_pool) {}
+  Scratch(marie_vie* hh, std::vector<std::pair<void*, size_t>>* p) : h(hh), pool(p) {}
   template <typename P>
   marie_status get(P** p, size_t count) {
     *p = nullptr;
     const size_t bytes = std::max<size_t>(count, 1) * sizeof(P);
+    std::vector<std::pair<void*, size_t>>& pl = *pool;
+    if (next < pl.size() && pl[next].second >= bytes) {
+      *p = (P*)pl[next++].first;
+      return MARIE_OK;
+    }
+    if (next < pl.size()) {     // too small: replace
+      cudaFree(pl[next].first);
+      h->mem_used -= (int64_t)pl[next].second;
+      pl[next] = {nullptr, 0};
+    }
     if (h->mem_cap > 0 && h->mem_used + (int64_t)bytes > h->mem_cap) {
       set_error("device memory cap exceeded by GMRES workspace (%zu bytes)", bytes);
       return MARIE_ERR_OOM;
     }
-    if (cudaMalloc((void**)p, bytes) != cudaSuccess) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
       cudaGetLastError();
       set_error("GMRES workspace allocation of %zu bytes failed", bytes);
       return MARIE_ERR_OOM;
     }
-    ptrs.push_back(*p);
+    h->mem_used += (int64_t)bytes;
+    if (next < pl.size()) pl[next] = {q, bytes};
+    else pl.push_back({q, bytes});
+    ++next;
+    *p = (P*)q;
     return MARIE_OK;
   }
 };
@@ -746,4 +763,93 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
   if (worst == MARIE_ERR_NOT_CONVERGED) set_error("some right-hand sides did not reach tol");
   if (worst == MARIE_ERR_NONFINITE) set_error("non-finite residual encountered");
   return (marie_status)worst;
+}
+
+// Host-buffer form: b and x in host memory (pinned for overlap).  The
+// right-hand sides are solved in chunks of the matvec chunk size through two
+// device buffer pairs: chunk k+1 is copied in before chunk k is solved, and
+// chunk k is copied out on a second stream while chunk k+1 is solved, so
+// only the first copy in and the last copy out are exposed.
+extern "C" marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, void* x_host, int32_t nrhs,
+                                             const marie_gmres_opts* o, marie_gmres_report* rep, void* stream) {
+  if (!h || !b_host || !x_host || !o) { set_error("NULL argument"); return MARIE_ERR_BAD_ARG; }
+  if (nrhs < 1) { set_error("nrhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
+  const int64_t Nb = h->Nb;
+  int cs = o->mode == MARIE_SOLVE_MIXED ? h->p32.ws_rhs : (h->p64.built ? h->p64.ws_rhs : h->pff.ws_rhs);
+  // MARIE_HOST_CHUNK: right-hand sides per chunk of the host-buffer solve
+  if (const char* e = getenv("MARIE_HOST_CHUNK")) {
+    if (atoi(e) > 0) cs = atoi(e);
+  }
+  cs = std::max(1, std::min(cs, (int)nrhs));
+  const int nch = (nrhs + cs - 1) / cs;
+  cudaStream_t s = (cudaStream_t)stream;
+  Scratch sc(h, &h->io_pool);
+  zd *bd[2] = {nullptr, nullptr}, *xd[2] = {nullptr, nullptr};
+  for (int i = 0; i < 2 && i < nch; ++i) {
+    MARIE_TRY(sc.get(&bd[i], (size_t)cs * Nb));
+    MARIE_TRY(sc.get(&xd[i], (size_t)cs * Nb));
+  }
+  cudaStream_t cps = nullptr;
+  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done = nullptr;
+  MARIE_CUDA_TRY(cudaStreamCreateWithFlags(&cps, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; ++i) cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming);
+  auto finish = [&](marie_status st) {
+    cudaStreamSynchronize(cps);
+    cudaStreamDestroy(cps);
+    for (int i = 0; i < 2; ++i) cudaEventDestroy(ev_in[i]);
+    cudaEventDestroy(ev_done);
+    return st;
+  };
+  const zd* bh = (const zd*)b_host;
+  zd* xh = (zd*)x_host;
+  auto copy_in = [&](int k) -> marie_status {
+    const int r0 = k * cs, nk = std::min(cs, nrhs - r0), u = k & 1;
+    const size_t bytes = sizeof(zd) * (size_t)nk * Nb;
+    if (cudaMemcpyAsync(bd[u], bh + (int64_t)r0 * Nb, bytes, cudaMemcpyHostToDevice, cps) != cudaSuccess ||
+        (o->x0_present && cudaMemcpyAsync(xd[u], xh + (int64_t)r0 * Nb, bytes, cudaMemcpyHostToDevice, cps) != cudaSuccess)) {
+      set_error("host-to-device copy of right-hand sides failed");
+      return MARIE_ERR_CUDA;
+    }
+    cudaEventRecord(ev_in[u], cps);
+    return MARIE_OK;
+  };
+  marie_status st = copy_in(0);
+  if (st != MARIE_OK) return finish(st);
+  int worst = MARIE_OK, mv64 = 0, mv32 = 0;
+  for (int k = 0; k < nch; ++k) {
+    const int r0 = k * cs, nk = std::min(cs, nrhs - r0), u = k & 1;
+    if (k + 1 < nch && (st = copy_in(k + 1)) != MARIE_OK) return finish(st);
+    cudaStreamWaitEvent(s, ev_in[u], 0);
+    marie_gmres_report sub = {};
+    if (rep) {
+      sub = *rep;
+      if (rep->iters) sub.iters = rep->iters + r0;
+      if (rep->outer) sub.outer = rep->outer + r0;
+      if (rep->last_inner) sub.last_inner = rep->last_inner + r0;
+      if (rep->true_resid) sub.true_resid = rep->true_resid + r0;
+      if (rep->resvec) sub.resvec = rep->resvec + (int64_t)r0 * rep->resvec_cap;
+      if (rep->resvec_len) sub.resvec_len = rep->resvec_len + r0;
+      if (rep->status) sub.status = rep->status + r0;
+    }
+    st = marie_gmres_vie(h, bd[u], xd[u], nk, o, rep ? &sub : nullptr, stream);
+    if (st != MARIE_OK && st != MARIE_ERR_NOT_CONVERGED && st != MARIE_ERR_NONFINITE) return finish(st);
+    if (st != MARIE_OK) worst = st;
+    mv64 += sub.matvecs_c128;
+    mv32 += sub.matvecs_c64;
+    cudaEventRecord(ev_done, s);
+    cudaStreamWaitEvent(cps, ev_done, 0);
+    if (cudaMemcpyAsync(xh + (int64_t)r0 * Nb, xd[u], sizeof(zd) * (size_t)nk * Nb, cudaMemcpyDeviceToHost, cps) !=
+        cudaSuccess) {
+      set_error("device-to-host copy of solutions failed");
+      return finish(MARIE_ERR_CUDA);
+    }
+  }
+  if (rep) {
+    rep->matvecs_c128 = mv64;
+    rep->matvecs_c64 = mv32;
+  }
+  if (worst == MARIE_ERR_NOT_CONVERGED) set_error("some right-hand sides did not reach tol");
+  if (worst == MARIE_ERR_NONFINITE) set_error("non-finite residual encountered");
+  return finish((marie_status)worst);
 }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <atomic>
+#include <utility>
 #include <string>
 #include <vector>
 #include <cstdio>
@@ -89,9 +90,11 @@ struct marie_vie {
   marie::PrecState<float> p32;
   marie::PrecState<marie::ff> pff;   // complex128 I/O, float-float arithmetic (precisions bit 4)
   std::vector<void*> allocs;
-  // GMRES scratch (allocated on first solve, grown on demand)
-  size_t gm_bytes = 0;
-  void* gm_base = nullptr;
+  // GMRES workspace pool: the buffers a solve requests, in request order,
+  // kept across solves and grown on demand (marie_vie_release_workspace
+  // frees them; destroy frees everything).
+  std::vector<std::pair<void*, size_t>> gm_pool;
+  std::vector<std::pair<void*, size_t>> io_pool;   // device buffers of the host-buffer solve
 };
 
 namespace marie {

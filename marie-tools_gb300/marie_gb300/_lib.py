@@ -71,6 +71,8 @@ _PROTOS = {
     "marie_vie_apply_K_adj": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, _vp]),
     "marie_gmres_vie": (ct.c_int, [_vp, _vp, _vp, ct.c_int32, ct.POINTER(GmresOpts),
                                    ct.POINTER(GmresReport), _vp]),
+    "marie_gmres_vie_host": (ct.c_int, [_vp, _vp, _vp, ct.c_int32, ct.POINTER(GmresOpts),
+                                        ct.POINTER(GmresReport), _vp]),
     "marie_assemble_green": (ct.c_int, [ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double,
                                         ct.c_int32, ct.c_int32, c_double_p]),
     "marie_incident_loops": (ct.c_int, [_vp, c_double_p, c_double_p, ct.c_int32, ct.c_double,
@@ -80,6 +82,7 @@ _PROTOS = {
                                              _vp]),
     "marie_vie_profile": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, ct.c_int32, c_double_p, _vp]),
     "marie_vie_tiles": (ct.c_int, [_vp, ct.c_int32, c_int32_p]),
+    "marie_vie_release_workspace": (ct.c_int, [_vp]),
     "marie_vie_fields": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, _vp, _vp, _vp, ct.c_int32, _vp]),
     "marie_vie_absorbed_power": (ct.c_int, [_vp, _vp, ct.c_int32, c_double_p, _vp]),
     "marie_vie_b1_plus": (ct.c_int, [_vp, _vp, ct.c_int32, _vp, _vp]),

@@ -111,6 +111,10 @@ class VieOperator:
         return None, _dptr(buf)
 
     # -- lifetime ---------------------------------------------------------
+    def release_workspace(self):
+        """Free the GMRES workspace kept between solves."""
+        check(self._lib.marie_vie_release_workspace(self._h))
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.marie_vie_destroy(self._h)
@@ -225,6 +229,23 @@ class VieOperator:
         return out
 
     # -- solve ----------------------------------------------------------------
+    def _run_gmres(self, fn, bptr, xptr, nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
+                   raise_on_fail):
+        o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol,
+                           mode=SOLVE_MIXED if mode == "mixed" else SOLVE_FP64,
+                           x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine)
+        it = np.zeros(nrhs, np.int32); ou = np.zeros(nrhs, np.int32); li = np.zeros(nrhs, np.int32)
+        tr = np.zeros(nrhs, np.float64); st = np.zeros(nrhs, np.int32); rl = np.zeros(nrhs, np.int32)
+        rv = np.zeros((nrhs, resvec_cap), np.float64)
+        ip = lambda a: a.ctypes.data_as(_lib.c_int32_p)
+        rep = _lib.GmresReport(iters=ip(it), outer=ip(ou), last_inner=ip(li), true_resid=_dptr(tr),
+                               resvec=_dptr(rv), resvec_cap=resvec_cap, resvec_len=ip(rl), status=ip(st))
+        s = fn(self._h, bptr, xptr, nrhs, ct.byref(o), ct.byref(rep), self._stream())
+        if s not in (0, 4) or (raise_on_fail and s != 0):
+            check(s)
+        return SolveReport(it, ou, li, tr, [rv[r, :rl[r]].copy() for r in range(nrhs)], st,
+                           rep.matvecs_c128, rep.matvecs_c64, ok=(s == 0))
+
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
               max_refine=10, resvec_cap=4096, raise_on_fail=False):
         """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA."""
@@ -236,21 +257,29 @@ class VieOperator:
         x0 = x is not None
         if x is None:
             x = torch.zeros_like(b)
-        o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol,
-                           mode=SOLVE_MIXED if mode == "mixed" else SOLVE_FP64,
-                           x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine)
-        it = np.zeros(nrhs, np.int32); ou = np.zeros(nrhs, np.int32); li = np.zeros(nrhs, np.int32)
-        tr = np.zeros(nrhs, np.float64); st = np.zeros(nrhs, np.int32); rl = np.zeros(nrhs, np.int32)
-        rv = np.zeros((nrhs, resvec_cap), np.float64)
-        ip = lambda a: a.ctypes.data_as(_lib.c_int32_p)
-        rep = _lib.GmresReport(iters=ip(it), outer=ip(ou), last_inner=ip(li), true_resid=_dptr(tr),
-                               resvec=_dptr(rv), resvec_cap=resvec_cap, resvec_len=ip(rl), status=ip(st))
-        s = self._lib.marie_gmres_vie(self._h, ct.c_void_p(b.data_ptr()), ct.c_void_p(x.data_ptr()), nrhs,
-                                      ct.byref(o), ct.byref(rep), self._stream())
-        if s not in (0, 4) or (raise_on_fail and s != 0):
-            check(s)
-        report = SolveReport(it, ou, li, tr, [rv[r, :rl[r]].copy() for r in range(nrhs)], st,
-                             rep.matvecs_c128, rep.matvecs_c64, ok=(s == 0))
+        report = self._run_gmres(self._lib.marie_gmres_vie, ct.c_void_p(b.data_ptr()), ct.c_void_p(x.data_ptr()),
+                                 nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
+                                 raise_on_fail)
+        return x, report
+
+    def gmres_host(self, b, x=None, *, out=None, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
+                   max_refine=10, resvec_cap=4096, raise_on_fail=False):
+        """is_gmres_vie on host buffers (marie_gmres_vie_host): b is a CPU
+        complex128 tensor (nrhs*N_b), page-locked for copy/compute overlap.
+        x (optional) holds x0 and receives the solution; otherwise the
+        solution goes to `out` (or a new tensor) from x0 = 0."""
+        import torch
+        if b.dtype != torch.complex128 or b.device.type != "cpu" or not b.is_contiguous():
+            raise ValueError("b must be a contiguous complex128 CPU tensor")
+        nrhs = b.numel() // self.Nb
+        x0 = x is not None
+        if x is None:
+            x = out if out is not None else torch.empty_like(b, pin_memory=b.is_pinned())
+        if x.dtype != torch.complex128 or x.device.type != "cpu" or not x.is_contiguous() or x.numel() != b.numel():
+            raise ValueError("x / out must match b")
+        report = self._run_gmres(self._lib.marie_gmres_vie_host, ct.c_void_p(b.data_ptr()),
+                                 ct.c_void_p(x.data_ptr()), nrhs, x0, restart, tol, maxit, mode, inner_tol,
+                                 max_refine, resvec_cap, raise_on_fail)
         return x, report
 
     # -- right-hand sides -----------------------------------------------------

@@ -106,3 +106,27 @@ def test_nonfinite_rhs_is_rejected():
     with pytest.raises(MarieError, match="NONFINITE"):
         op.gmres(torch.from_numpy(b).cuda(), restart=10, tol=1e-8, mode="fp64")
     op.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_host_buffer_solve_equals_device_solve(mode):
+    """marie_gmres_vie_host (chunked, copies overlapped) returns the device
+    solve's result for every right-hand side, with and without x0, and with
+    more right-hand sides than one chunk."""
+    op, A, mv, dims, emc, ep = _case("pwl_4")
+    rng = np.random.default_rng(5)
+    nrhs = 7
+    B = np.stack([mv["b"] * (1 + 0.1 * r) + 0.01 * (rng.normal(size=mv["b"].size) + 1j * rng.normal(size=mv["b"].size))
+                  for r in range(nrhs)])
+    bd = torch.from_numpy(B.reshape(-1)).cuda()
+    xd, repd = op.gmres(bd, restart=20, tol=1e-8, mode=mode)
+    bh = torch.from_numpy(B.reshape(-1)).pin_memory()
+    xh, reph = op.gmres_host(bh, restart=20, tol=1e-8, mode=mode)
+    assert np.array_equal(xh.numpy(), xd.cpu().numpy())
+    assert np.array_equal(reph.iters, repd.iters) and np.array_equal(reph.true_resid, repd.true_resid)
+    x0 = (0.5 * xd).cpu().contiguous()
+    xh2, _ = op.gmres_host(bh, x0.clone(), restart=20, tol=1e-8, mode=mode)
+    xd2, _ = op.gmres(bd, (0.5 * xd).contiguous(), restart=20, tol=1e-8, mode=mode)
+    assert np.array_equal(xh2.numpy(), xd2.cpu().numpy())
+    op.close()
