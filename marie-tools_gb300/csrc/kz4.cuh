@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   const int kyp = blockIdx.z, k0 = blockIdx.y * a.TX;
   const int n1 = a.n1, n2 = a.n2, m1 = 2 * n1, R = a.R;
   const int W = a.TX * R, wl = min(a.TX, m1 - k0) * R;
+  const int lgW = 31 - __clz(W);                // W = TX*R is a power of two
   const int S = kz4_stride(N, W);
   const int H = C * W * S + kz4_halfpad(W);   // start of the odd half
   const int T1 = 2 * C * NB * W;              // tasks of forward step 1 / inverse step B
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // 2N-point transform (h = 1: inputs times w_2N^z), 16-point DFT over a of
   // z = NB*a + b, then the four-step twiddle.
   for (int t = threadIdx.x; t < T1; t += blockDim.x) {
-    const int e = t % W, r = t / W;
+    const int e = t & (W - 1), r = t >> lgW;
     const int h = r & 1, r2 = r >> 1;
     const int b = r2 % NB, c = r2 / NB;
     const unsigned live = a.zq ? a.zq[b] : 0xffffu;   // slices z = NB*q + b
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // forward step 2 (in place): task (s, k1), k1 fastest; NB-point DFT
   for (int t = threadIdx.x; t < 2 * C * W * 16; t += blockDim.x) {
     const int k1 = t & 15, s = t >> 4;
-    const int h = s / (C * W);
+    const int h = s >= C * W ? 1 : 0;
     cplx<T>* p = buf + h * H + (s - h * C * W) * S;
     cplx<T> w[NB];
 #pragma unroll
@@ -235,12 +236,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   constexpr int U = OpTab<PWL, OP>::L.nblk;
   const int beta = kyp / n2, ky = 2 * (kyp - beta * n2) + beta;
   for (int i = threadIdx.x; i < 2 * N * W; i += blockDim.x) {
-    const int e = i % W, pp = i / W;
-    const int kxp = k0 + e / R;
+    const int e = i & (W - 1), pp = i >> lgW;
+    const int kxp = k0 + (e >> a.lgR);
     if (kxp >= m1) continue;
     const int g = pp / N, k = pp - g * N;
     const int kz = 2 * k + g;
-    const int alpha = kxp / n1;
+    const int alpha = kxp >= n1 ? 1 : 0;
     const int kx = 2 * (kxp - alpha * n1) + alpha;
     const cplx<T>* gp = a.G + (((int64_t)ky * m1 + kx) * (2 * N) + kz) * U;
     cplx<T>* v = buf + g * H + e * S + zpos(k >> 4, k & 15);
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // inverse step A (in place): task (s, k1), k1 fastest
   for (int t = threadIdx.x; t < 2 * C * W * 16; t += blockDim.x) {
     const int k1 = t & 15, s = t >> 4;
-    const int h = s / (C * W);
+    const int h = s >= C * W ? 1 : 0;
     cplx<T>* p = buf + h * H + (s - h * C * W) * S;
     cplx<T> w[NB];
 #pragma unroll
@@ -267,14 +268,15 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // half h (h = 1 then times conj(w_2N^z)).  The partner lane t ^ W holds the
   // other half of the same (e, b, c): the even lane stores q < 8, the odd lane
   // q >= 8, after one exchange.  The loop is warp-uniform so that every lane
-  // takes part in the shuffles; lanes past T1 redo a valid task (tasks come
-  // in aligned groups of 2W, so t mod T1 keeps (e, h)) and store nothing.
+  // takes part in the shuffles; lanes past T1 redo a valid task of the first
+  // group (tasks come in aligned groups of 2W, so t & (2W - 1) keeps (e, h)
+  // and pairs partners again) and store nothing.
   const int lane = threadIdx.x & 31;
   for (int tb = threadIdx.x - lane; tb < T1; tb += blockDim.x) {
     const int t = tb + lane;
     const bool act = t < T1;
-    const int tt = act ? t : t % T1;
-    const int e = tt % W, r = tt / W;
+    const int tt = act ? t : (t & (2 * W - 1));   // a valid task with the same (e, h)
+    const int e = tt & (W - 1), r = tt >> lgW;
     const int h = r & 1, r2 = r >> 1;
     const int b = r2 % NB, c = r2 / NB;
     const cplx<T>* sp = buf + h * H + (c * W + e) * S + b * 16;

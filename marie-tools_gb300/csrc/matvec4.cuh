@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_y(MvArgs<T
   if (!z_is_live(a, z)) return;   // slice without body voxels: the z pass reads it as zero
   const int n1 = a.n1, n3 = a.n3, m1 = 2 * n1, R = a.R;
   const int W = a.TXY * R, wl = min(a.TXY, m1 - k0) * R;
+  const int lgW = 31 - __clz(W);   // TXY*R is a power of two
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + N;
   load_tw(tw, a.ay.tw, N);
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_y(MvArgs<T
   const cplx<T>* src = a.T1 + (((int64_t)bu * a.C + c) * n3 + z) * (int64_t)N * row + (int64_t)k0 * R;
   // step 1: task (b, e), e fastest
   for (int t = threadIdx.x; t < W * NB; t += blockDim.x) {
-    const int e = t % W, b = t / W;
+    const int e = t & (W - 1), b = t >> lgW;
     const unsigned live = a.rowq ? a.rowq[z * 8 + b] : 0xffffu;   // rows y = NB*q + b
     cplx<T> v[16], u[16];
 #pragma unroll
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_y(MvArgs<T
   // step 2: task (beta, k1, e), e fastest; S_glob[bu][c][beta*N + k][z][kx'][r]
   cplx<T>* dst = a.S + ((int64_t)bu * a.C + c) * (int64_t)2 * N * n3 * row + (int64_t)k0 * R;
   for (int t = threadIdx.x; t < 2 * 16 * W; t += blockDim.x) {
-    const int e = t % W, q = t / W;
+    const int e = t & (W - 1), q = t >> lgW;
     const int k1 = q & 15, beta = q >> 4;
     cplx<T> w[NB];
 #pragma unroll
@@ -305,6 +306,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
   if (!z_is_live(a, z)) return;   // no body voxel in slice z: no output
   const int n1 = a.n1, n3 = a.n3, m1 = 2 * n1, R = a.R;
   const int W = a.TXY * R, wl = min(a.TXY, m1 - k0) * R;
+  const int lgW = 31 - __clz(W);   // TXY*R is a power of two
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + N;
   load_tw(tw, a.ay.tw, N);
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
   const cplx<T>* src = a.S + ((int64_t)bu * a.C + c) * (int64_t)2 * N * n3 * row + (int64_t)k0 * R;
   // step A: task (beta, k1, e)
   for (int t = threadIdx.x; t < 2 * 16 * W; t += blockDim.x) {
-    const int e = t % W, q = t / W;
+    const int e = t & (W - 1), q = t >> lgW;
     const int k1 = q & 15, beta = q >> 4;
     cplx<T> w[NB];
 #pragma unroll
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
   // step B: task (b, e): inverse 16-point DFTs of both halves, combine, store
   cplx<T>* dst = a.T1 + (((int64_t)bu * a.C + c) * n3 + z) * (int64_t)N * row + (int64_t)k0 * R;
   for (int t = threadIdx.x; t < W * NB; t += blockDim.x) {
-    const int e = t % W, b = t / W;
+    const int e = t & (W - 1), b = t >> lgW;
     const unsigned live = a.rowq ? a.rowq[z * 8 + b] : 0xffffu;   // rows y = NB*q + b
     cplx<T> u0[16], u1[16];
 #pragma unroll
