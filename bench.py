@@ -148,10 +148,9 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
     green = U * (n + 1) ** 3 * s            # octant spectrum, read once per launch
     alg = units * per_rhs + green
     achieved = alg / (ms_z * 1e-3) / 1e9
-    # ncu dram bytes per right-hand side of one z-pass launch (profiles/k_z_c64_pwl128.md), scaled to the launch
-    traffic = None
-    if ZTRAFFIC_PER_RHS is not None and wl["pwl"] and n == 128:
-        traffic = ZTRAFFIC_PER_RHS * units + green
+    # ncu dram bytes (read + write) of one 16-RHS z-pass launch of this
+    # workload (profiles/k4_z_c64_128pwl_16rhs_dram.md)
+    traffic = ZTRAFFIC_128PWL_16RHS if (wl["pwl"] and n == 128 and units == 16) else None
     four_step = n % 16 == 0 and 16 <= n <= 128
     name = (f"k4_z<float,{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
     return {"kernel": name + " (z FFT + Green block multiply + inverse z FFT)", "bound": "hbm",
@@ -160,7 +159,7 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
             "units_per_launch": units, "peak_source": peak_kind}
 
 
-ZTRAFFIC_PER_RHS = None
+ZTRAFFIC_128PWL_16RHS = 26.14e9
 
 
 def run_ours(args, wl):
