@@ -128,9 +128,11 @@ typedef struct {
   double tol;             /* relative residual target */
   int32_t mode;           /* marie_solve_mode */
   int32_t x0_present;     /* 1: x holds the initial guess; 0: start from zero */
-  double inner_tol;       /* MIXED: floor of the inner c64 GMRES relative tolerance (0 = 1e-7);
-                             each inner solve asks for max(inner_tol, 0.3*tol/current residual) */
-  int32_t max_refine;     /* MIXED: max refinement steps */
+  double inner_tol;       /* MIXED: floor of the inner c64 GMRES relative tolerance (0 = 1e-7) */
+  int32_t max_refine;     /* MIXED: max refinement steps (0 = 10) */
+  double inner_safety;    /* MIXED: each inner solve asks for
+                             clamp(inner_safety*tol/current residual, inner_tol, 0.5) (0 = 0.9);
+                             the FP64 true residual decides convergence either way */
 } marie_gmres_opts;
 
 typedef struct {

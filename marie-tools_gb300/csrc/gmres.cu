@@ -720,6 +720,11 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
     }
     const double floor_tol = o->inner_tol > 0 ? o->inner_tol : 1e-7;
     const int max_refine = o->max_refine > 0 ? o->max_refine : 10;
+    // fraction of the outer target the inner solve aims for: 0.9 takes the
+    // complex64 solve to 13 iterations at 128^3 PWL (0.3: 14) with true
+    // residuals <= 7e-7 for tol 1e-6; a right-hand side that still misses
+    // tol gets another (short) inner solve
+    const double safety = o->inner_safety > 0 ? o->inner_safety : 0.9;
     for (int it = 0; it < max_refine; ++it) {
       std::vector<unsigned char> todo(nrhs, 0);
       int n = 0;
@@ -736,7 +741,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
       std::vector<double> rn(nrhs), tin(nrhs);
       for (int r = 0; r < nrhs; ++r) {
         rn[r] = rel[r] * bnorm[r];
-        tin[r] = std::min(0.5, std::max(floor_tol, 0.3 * o->tol / std::max(rel[r], 1e-300)));
+        tin[r] = std::min(0.5, std::max(floor_tol, safety * o->tol / std::max(rel[r], 1e-300)));
       }
       std::vector<RhsLog> ilog(nrhs);
       MARIE_TRY(gmres_core<float>(h, nrhs, V, m, x, rn, tin, o->maxit, todo, ilog, &mv32, s, sc));

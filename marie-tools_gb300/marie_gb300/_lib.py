@@ -49,7 +49,8 @@ class VieDesc(ct.Structure):
 
 class GmresOpts(ct.Structure):
     _fields_ = [("restart", ct.c_int32), ("maxit", ct.c_int32), ("tol", ct.c_double), ("mode", ct.c_int32),
-                ("x0_present", ct.c_int32), ("inner_tol", ct.c_double), ("max_refine", ct.c_int32)]
+                ("x0_present", ct.c_int32), ("inner_tol", ct.c_double), ("max_refine", ct.c_int32),
+                ("inner_safety", ct.c_double)]
 
 
 class GmresReport(ct.Structure):

@@ -230,10 +230,11 @@ class VieOperator:
 
     # -- solve ----------------------------------------------------------------
     def _run_gmres(self, fn, bptr, xptr, nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
-                   raise_on_fail):
+                   raise_on_fail, inner_safety=0.0):
         o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol,
                            mode=SOLVE_MIXED if mode == "mixed" else SOLVE_FP64,
-                           x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine)
+                           x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine,
+                           inner_safety=inner_safety)
         it = np.zeros(nrhs, np.int32); ou = np.zeros(nrhs, np.int32); li = np.zeros(nrhs, np.int32)
         tr = np.zeros(nrhs, np.float64); st = np.zeros(nrhs, np.int32); rl = np.zeros(nrhs, np.int32)
         rv = np.zeros((nrhs, resvec_cap), np.float64)
@@ -247,7 +248,7 @@ class VieOperator:
                            rep.matvecs_c128, rep.matvecs_c64, ok=(s == 0))
 
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
-              max_refine=10, resvec_cap=4096, raise_on_fail=False):
+              max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0):
         """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA."""
         import torch
         b = b.contiguous()
@@ -259,11 +260,11 @@ class VieOperator:
             x = torch.zeros_like(b)
         report = self._run_gmres(self._lib.marie_gmres_vie, ct.c_void_p(b.data_ptr()), ct.c_void_p(x.data_ptr()),
                                  nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
-                                 raise_on_fail)
+                                 raise_on_fail, inner_safety)
         return x, report
 
     def gmres_host(self, b, x=None, *, out=None, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
-                   max_refine=10, resvec_cap=4096, raise_on_fail=False):
+                   max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0):
         """is_gmres_vie on host buffers (marie_gmres_vie_host): b is a CPU
         complex128 tensor (nrhs*N_b), page-locked for copy/compute overlap.
         x (optional) holds x0 and receives the solution; otherwise the
@@ -279,7 +280,7 @@ class VieOperator:
             raise ValueError("x / out must match b")
         report = self._run_gmres(self._lib.marie_gmres_vie_host, ct.c_void_p(b.data_ptr()),
                                  ct.c_void_p(x.data_ptr()), nrhs, x0, restart, tol, maxit, mode, inner_tol,
-                                 max_refine, resvec_cap, raise_on_fail)
+                                 max_refine, resvec_cap, raise_on_fail, inner_safety)
         return x, report
 
     # -- right-hand sides -----------------------------------------------------

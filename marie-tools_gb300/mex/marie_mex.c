@@ -171,8 +171,9 @@ static void cmd_gmres(int nlhs, mxArray** plhs, int nrhs, const mxArray** prhs, 
   o.tol = scalar(prhs[4], "tol");
   o.maxit = (int32_t)scalar(prhs[5], "maxit");
   o.mode = nrhs > 7 ? (int32_t)scalar(prhs[7], "mode") : MARIE_SOLVE_FP64;
-  o.inner_tol = 1e-5;
-  o.max_refine = 10;
+  o.inner_tol = 0.0;      /* library defaults */
+  o.max_refine = 0;
+  o.inner_safety = 0.0;
   const mxArray* X0 = prhs[6];
   void *db = NULL, *dx = NULL;
   if (cudaMalloc(&db, (size_t)n * 16) || cudaMalloc(&dx, (size_t)n * 16)) mexErrMsgIdAndTxt("marie:OOM", "device allocation failed");
