@@ -175,11 +175,11 @@ static void cmd_gmres(int nlhs, mxArray** plhs, int nrhs, const mxArray** prhs, 
   o.max_refine = 0;
   o.inner_safety = 0.0;
   const mxArray* X0 = prhs[6];
-  void *db = NULL, *dx = NULL;
-  if (cudaMalloc(&db, (size_t)n * 16) || cudaMalloc(&dx, (size_t)n * 16)) mexErrMsgIdAndTxt("marie:OOM", "device allocation failed");
-  cudaMemcpy(db, mxGetComplexDoubles(B), (size_t)n * 16, H2D);
+  /* the solution array doubles as x0: the host-buffer solve reads it when
+     x0_present and overwrites it with the solution */
+  plhs[0] = mxCreateNumericArray(mxGetNumberOfDimensions(B), mxGetDimensions(B), mxDOUBLE_CLASS, mxCOMPLEX);
   if (!mxIsEmpty(X0) && mxIsComplex(X0) && (int64_t)mxGetNumberOfElements(X0) == n) {
-    cudaMemcpy(dx, mxGetComplexDoubles(X0), (size_t)n * 16, H2D);
+    memcpy(mxGetComplexDoubles(plhs[0]), mxGetComplexDoubles(X0), (size_t)n * 16);
     o.x0_present = 1;
   }
   const int cap = o.restart * (o.maxit > 0 ? o.maxit : 1) + 1;
@@ -194,11 +194,8 @@ static void cmd_gmres(int nlhs, mxArray** plhs, int nrhs, const mxArray** prhs, 
   rep.resvec = rv;
   rep.resvec_cap = cap;
   rep.resvec_len = rlen;
-  marie_status s = marie_gmres_vie(h, db, dx, k, &o, &rep, NULL);
-  plhs[0] = mxCreateNumericArray(mxGetNumberOfDimensions(B), mxGetDimensions(B), mxDOUBLE_CLASS, mxCOMPLEX);
-  cudaMemcpy(mxGetComplexDoubles(plhs[0]), dx, (size_t)n * 16, D2H);
-  cudaFree(db);
-  cudaFree(dx);
+  /* host arrays straight into the chunked host-buffer solve */
+  marie_status s = marie_gmres_vie_host(h, mxGetComplexDoubles(B), mxGetComplexDoubles(plhs[0]), k, &o, &rep, NULL);
   if (s != MARIE_OK && s != MARIE_ERR_NOT_CONVERGED) check(s);
   if (nlhs > 1) {
     plhs[1] = mxCreateDoubleMatrix(k, 2, mxREAL);   /* iter = [p outit] per rhs */
