@@ -186,6 +186,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   const int S = kz4_stride(N, W);
   const int H = C * W * S + kz4_halfpad(W);   // start of the odd half
   const int T1 = 2 * C * NB * W;              // tasks of forward step 1 / inverse step B
+  // two tasks' loads in flight per thread for complex64; float-float keeps
+  // one (its larger code already strains the instruction cache)
+  constexpr int kTaskUnroll = std::is_same<T, float>::value ? 2 : 1;
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + N;
   load_tw(tw, a.az.tw, N);
@@ -197,6 +200,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // forward step 1: task (e, h, b, c), e fastest; half h of the zero-padded
   // 2N-point transform (h = 1: inputs times w_2N^z), 16-point DFT over a of
   // z = NB*a + b, then the four-step twiddle.
+#pragma unroll kTaskUnroll
   for (int t = threadIdx.x; t < T1; t += blockDim.x) {
     const int e = t & (W - 1), r = t >> lgW;
     const int h = r & 1, r2 = r >> 1;
@@ -272,6 +276,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // group (tasks come in aligned groups of 2W, so t & (2W - 1) keeps (e, h)
   // and pairs partners again) and store nothing.
   const int lane = threadIdx.x & 31;
+#pragma unroll kTaskUnroll
   for (int tb = threadIdx.x - lane; tb < T1; tb += blockDim.x) {
     const int t = tb + lane;
     const bool act = t < T1;
