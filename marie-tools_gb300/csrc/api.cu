@@ -281,11 +281,6 @@ static marie_status alloc_workspace(marie_vie* h, PrecState<T>& ps) {
 }
 
 template <typename T>
-static void set_smem_attr(const void* fn) {
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-}
-
-template <typename T>
 static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<typename IoOf<T>::type>* in,
                                      int64_t in_rs, cplx<typename IoOf<T>::type>* out, int64_t out_rs, int nrhs,
                                      const unsigned char* active, cudaStream_t stream, cudaEvent_t* ev,
@@ -293,10 +288,8 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
 
 template <typename T, bool PWL, int OP>
 static void launch_z(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    cudaFuncSetAttribute((const void*)k_z<T, PWL, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  });
+  static std::atomic<uint64_t> done{0};
+  smem_opt_in_device((const void*)k_z<T, PWL, OP>, done);
   k_z<T, PWL, OP><<<g, 256, smem, s>>>(a);
 }
 
@@ -348,17 +341,15 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
     set_error("K operator was not supplied at create time");
     return MARIE_ERR_BAD_ARG;
   }
-  static std::once_flag once;
-  std::call_once(once, [] {
-    set_smem_attr<T>((const void*)k_fwd_x<float>);
-    set_smem_attr<T>((const void*)k_fwd_y<float>);
-    set_smem_attr<T>((const void*)k_inv_y<float>);
-    set_smem_attr<T>((const void*)k_inv_x<float>);
-    set_smem_attr<T>((const void*)k_fwd_x<double>);
-    set_smem_attr<T>((const void*)k_fwd_y<double>);
-    set_smem_attr<T>((const void*)k_inv_y<double>);
-    set_smem_attr<T>((const void*)k_inv_x<double>);
-  });
+  static std::atomic<uint64_t> done[8];
+  smem_opt_in_device((const void*)k_fwd_x<float>, done[0]);
+  smem_opt_in_device((const void*)k_fwd_y<float>, done[1]);
+  smem_opt_in_device((const void*)k_inv_y<float>, done[2]);
+  smem_opt_in_device((const void*)k_inv_x<float>, done[3]);
+  smem_opt_in_device((const void*)k_fwd_x<double>, done[4]);
+  smem_opt_in_device((const void*)k_fwd_y<double>, done[5]);
+  smem_opt_in_device((const void*)k_inv_y<double>, done[6]);
+  smem_opt_in_device((const void*)k_inv_x<double>, done[7]);
   MvArgs<T> a;
   memset(&a, 0, sizeof(a));
   a.n1 = h->n1;

@@ -1,7 +1,7 @@
 // Definitions of the four-step pass launchers declared in fastpath.cuh.
 #pragma once
 
-#include <mutex>
+#include <atomic>
 
 #include "fastpath.cuh"
 #include "matvec4.cuh"
@@ -9,15 +9,13 @@
 namespace marie {
 
 template <typename KernelFn>
-static void smem_opt_in(KernelFn fn, std::once_flag& once) {
-  std::call_once(once, [fn] {
-    cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  });
+static void smem_opt_in(KernelFn fn, std::atomic<uint64_t>& done) {
+  smem_opt_in_device((const void*)fn, done);
 }
 
 template <typename T, int NB>
 static void launch_x(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag of, oi;
+  static std::atomic<uint64_t> of{0}, oi{0};
   if (!inv) {
     smem_opt_in(k4_fwd_x<T, NB>, of);
     k4_fwd_x<T, NB><<<g, 256, smem, s>>>(a);
@@ -29,7 +27,7 @@ static void launch_x(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStre
 
 template <typename T, int NB>
 static void launch_y(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag of, oi;
+  static std::atomic<uint64_t> of{0}, oi{0};
   if (!inv) {
     smem_opt_in(k4_fwd_y<T, NB>, of);
     k4_fwd_y<T, NB><<<g, 256, smem, s>>>(a);
@@ -41,7 +39,7 @@ static void launch_y(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStre
 
 template <typename T, int NB, bool PWL, int OP>
 static void launch_z4(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
-  static std::once_flag o;
+  static std::atomic<uint64_t> o{0};
   smem_opt_in(k4_z<T, NB, PWL, OP>, o);
   k4_z<T, NB, PWL, OP><<<g, 256, smem, s>>>(a);
 }

@@ -129,6 +129,19 @@ marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaS
 
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
 
+// Opt a kernel into the large dynamic shared-memory carve-out once per
+// device (the attribute is per device; a process may drive several).
+// `done` is the kernel's own flag word: bit d set once device d is done.
+constexpr int kMaxDevices = 64;
+inline void smem_opt_in_device(const void* fn, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = 1ull << (dev & (kMaxDevices - 1));
+  if (done.load(std::memory_order_acquire) & bit) return;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
 // Every grid edge is 16*NB with NB <= 8: the four-step passes apply.
 inline bool four_step_edge(int n) { return n % 16 == 0 && n / 16 >= 1 && n / 16 <= 8; }
 inline bool four_step_grid(const marie_vie* h) {
