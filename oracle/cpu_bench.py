@@ -1,6 +1,6 @@
 """Timed CPU baseline: the FP64 reference algorithm on the host cores.
 
-TEST / BASELINE INFRASTRUCTURE ONLY (used by bench.py's cpu_baseline leg and
+TEST AND CPU-BASELINE INFRASTRUCTURE ONLY (used by bench.py's cpu_baseline leg and
 its reference arm).  The reference path is MATLAB (fftn, elementwise MACs,
 mldivide); MATLAB is unavailable, so the same algorithm is timed as a
 numpy/scipy port using every host core:
