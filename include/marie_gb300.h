@@ -133,6 +133,8 @@ typedef struct {
   double inner_safety;    /* MIXED: each inner solve asks for
                              clamp(inner_safety*tol/current residual, inner_tol, 0.5) (0 = 0.9);
                              the FP64 true residual decides convergence either way */
+  int32_t adjoint;        /* 1: solve A^H x = b (A^H as marie_vie_apply_adjoint), for adjoint
+                             sensitivities; 0: A x = b */
 } marie_gmres_opts;
 
 typedef struct {
@@ -199,6 +201,25 @@ marie_status marie_vie_fields(marie_vie* h, int32_t prec, const void* J, const v
  * phi_host: host, nrhs x nrhs complex128 (row p, column q), FP64 sums in a
  * fixed order. */
 marie_status marie_vie_absorbed_power(marie_vie* h, const void* J, int32_t nrhs, double* phi_host, void* stream);
+/* Adjoint of the H-field map of marie_vie_fields: y = K^H(invG x) on the
+ * body (x, y: body vectors, nrhs x N_b).  Needs the K operator.  Used for
+ * the adjoint source of B1+ objectives. */
+marie_status marie_vie_apply_hfield_adjoint(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs,
+                                            void* stream);
+/* Adjoint sensitivities of J_obj = M/P with M = mean_ROI |B1+|^2 and P the
+ * absorbed power (1/2) phi(1,1) of one solved current J (device complex128
+ * body vectors, one right-hand side):
+ *   marie_vie_gradient_source: g = gM/P - (M/P^2)(1/2) D J, gM = dM/dconj(J),
+ *     D = G real(Mc_inv/ce) (the adjoint equation A^H lam = g follows, GMRES
+ *     with opts.adjoint = 1);
+ *   marie_vie_gradient: dJ_obj/d eps_r and dJ_obj/d sigma per body voxel
+ *     (device double, N_s each) from J, lam and the total field E of
+ *     marie_vie_fields.
+ * No counterpart in the reference: the derivation is in csrc/fields.cu. */
+marie_status marie_vie_gradient_source(marie_vie* h, const void* J, const void* gM, double M, double P, void* g,
+                                       void* stream);
+marie_status marie_vie_gradient(marie_vie* h, const void* J, const void* lam, const void* E, double M, double P,
+                                double* d_eps, double* d_sigma, void* stream);
 /* B1+ = mu0 (H_x + i H_y) on the constant moment of each body voxel
  * (em_ehfield_vie.m:68).  H: device complex128, nrhs x N_b; out: device
  * complex128, nrhs x N_s. */

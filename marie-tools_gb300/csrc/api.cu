@@ -589,6 +589,7 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   // contrast chi = (1./Mr).*Mc on the body (mvp_vie.m:17)
   std::vector<cplx<double>> chi(h->Ns);
   std::vector<double> wpow(h->Ns);
+  std::vector<cplx<double>> mrb(h->Ns);
   for (int64_t s = 0; s < h->Ns; ++s) {
     const std::complex<double> Mr(d->Mr[2 * idxS[s]], d->Mr[2 * idxS[s] + 1]);
     if (!std::isfinite(Mr.real()) || !std::isfinite(Mr.imag()) || Mr == 0.0) {
@@ -600,7 +601,10 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
     chi[s] = cplx<double>{v.real(), v.imag()};
     // real(Mc_inv / ce), the absorbed-power weight of em_ehfield_vie.m:46 (0 where Mc = 0)
     wpow[s] = Mc == 0.0 ? 0.0 : ((1.0 / Mc) / std::complex<double>(0.0, h->ce_im)).real();
+    mrb[s] = cplx<double>{Mr.real(), Mr.imag()};
   }
+  if ((st = dev_alloc(h, (void**)&h->mr_body, h->Ns * sizeof(cplx<double>))) != MARIE_OK) return fail(st);
+  cudaMemcpy(h->mr_body, mrb.data(), h->Ns * sizeof(cplx<double>), cudaMemcpyHostToDevice);
   if ((st = dev_alloc(h, (void**)&h->wpow, h->Ns * sizeof(double))) != MARIE_OK) return fail(st);
   cudaMemcpy(h->wpow, wpow.data(), h->Ns * sizeof(double), cudaMemcpyHostToDevice);
   (void)e0;
@@ -701,6 +705,10 @@ marie_status marie_vie_apply_K(marie_vie* h, int32_t prec, const void* x, void* 
 }
 marie_status marie_vie_apply_K_adj(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream) {
   return apply_common(h, prec, x, y, nrhs, stream, MV_GRID, OP_K_ADJ);
+}
+marie_status marie_vie_apply_hfield_adjoint(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs,
+                                            void* stream) {
+  return apply_common(h, prec, x, y, nrhs, stream, MV_HFIELD_ADJ, OP_K_ADJ);
 }
 
 marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,

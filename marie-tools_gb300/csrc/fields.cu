@@ -83,6 +83,60 @@ __global__ void k_b1_plus(const zd* H, int64_t Nb, int64_t Ns, int l, int nrhs, 
   out[(int64_t)r * Ns + s] = zd{mu0 * (hx.x - hy.y), mu0 * (hx.y + hy.x)};
 }
 
+// Adjoint sensitivities of J_obj = M / P, M = mean over an ROI of |B1+|^2,
+// P = (1/2) sum |J|^2 g_c real(Mc_inv/ce) (the absorbed power, phi(p,p)/2),
+// with respect to each body voxel's eps_r and sigma.  With the VIE system
+// A J = b, A = I - diag(chi) invG N, chi = 1 - 1/Mr, b = ce chi Ue and
+// Mr = eps_r + sigma/ce:
+//   g      = dJ_obj/dconj(J) = gM / P - (M / P^2) (1/2) D J,   D = g_c real(Mc_inv/ce)
+//   A^H lam = g
+//   dJ_obj/dp_s = 2 Re( sum_c conj(lam_cs) (ce E_cs + J_cs) (dMr/dp)/Mr_s^2 )
+//               + (M / P^2) (1/2) sum_c |J_cs|^2 g_c Re( (dMr/dp) / ((Mr_s - 1)^2 ce) )
+// where E is the total field of marie_vie_fields (ce E + J = ce Ue + invG N J)
+// and gM = dM/dconj(J) = (mu0/|ROI|) (invG K)^H w (marie_vie_apply_hfield_adjoint).
+
+// g = gM/P - (M/P^2)(1/2) D J
+__global__ void k_grad_source(const zd* J, const zd* gM, int64_t Nb, int64_t Ns, const double* wpow,
+                              const double* gdiag, double invP, double c2, zd* g) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= Nb) return;
+  const double d = wpow[i % Ns] * gdiag[i / Ns] * c2;
+  g[i] = zd{gM[i].x * invP - d * J[i].x, gM[i].y * invP - d * J[i].y};
+}
+
+__global__ void k_grad(const zd* J, const zd* lam, const zd* E, int64_t Ns, int C, const double* gdiag,
+                       const zd* mr, double ce_im, double expl, double* deps, double* dsig) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= Ns) return;
+  zd q = {0, 0};
+  double jj = 0;
+  for (int c = 0; c < C; ++c) {
+    const int64_t i = (int64_t)c * Ns + s;
+    const zd ceE = {-ce_im * E[i].y, ce_im * E[i].x};       // ce = i ce_im
+    const zd t = ceE + J[i];
+    q = q + zd{lam[i].x * t.x + lam[i].y * t.y, lam[i].x * t.y - lam[i].y * t.x};   // conj(lam) t
+    jj += (J[i].x * J[i].x + J[i].y * J[i].y) * gdiag[c];
+  }
+  const zd m = mr[s];
+  const zd m2 = m * m;
+  const double n2 = m2.x * m2.x + m2.y * m2.y;
+  const zd inv_m2 = {m2.x / n2, -m2.y / n2};                // 1/Mr^2
+  const zd inv_ce = {0, -1.0 / ce_im};                      // 1/ce
+  const zd a = q * inv_m2;
+  deps[s] = 2.0 * a.x;
+  dsig[s] = 2.0 * (a * inv_ce).x;
+  const zd mc = {m.x - 1.0, m.y};
+  const zd mc2 = mc * mc;
+  const double nc = mc2.x * mc2.x + mc2.y * mc2.y;
+  if (nc > 0) {
+    const zd inv_mc2 = {mc2.x / nc, -mc2.y / nc};            // 1/(Mr - 1)^2
+    const zd e1 = inv_mc2 * inv_ce;                          // dMr/deps = 1
+    const zd e2 = e1 * inv_ce;                               // dMr/dsigma = 1/ce
+    deps[s] += expl * jj * e1.x;
+    dsig[s] += expl * jj * e2.x;
+  }
+}
+
 }  // namespace marie
 
 using namespace marie;
@@ -155,6 +209,57 @@ marie_status marie_vie_b1_plus(marie_vie* h, const void* H, int32_t nrhs, void* 
   k_b1_plus<<<grid, 256, 0, s>>>((const zd*)H, h->Nb, h->Ns, h->pwl ? 4 : 1, nrhs, mu0, (zd*)out);
   g_launches++;
   if (cudaGetLastError() != cudaSuccess) { set_error("B1+ kernel launch failed"); return MARIE_ERR_CUDA; }
+  return MARIE_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+static marie_status upload_gdiag(marie_vie* h, double** gd, cudaStream_t s) {
+  double g[12];
+  for (int c = 0; c < h->C; ++c) g[c] = 1.0 / h->invg[c];
+  if (cudaMalloc((void**)gd, h->C * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("device allocation failed");
+    return MARIE_ERR_OOM;
+  }
+  cudaMemcpyAsync(*gd, g, h->C * sizeof(double), cudaMemcpyHostToDevice, s);
+  return MARIE_OK;
+}
+
+marie_status marie_vie_gradient_source(marie_vie* h, const void* J, const void* gM, double M, double P, void* g,
+                                       void* stream) {
+  if (!h || !J || !gM || !g || !(P > 0)) { set_error("marie_vie_gradient_source: invalid argument"); return MARIE_ERR_BAD_ARG; }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* gd = nullptr;
+  MARIE_TRY(upload_gdiag(h, &gd, s));
+  k_grad_source<<<(unsigned)((h->Nb + 255) / 256), 256, 0, s>>>((const zd*)J, (const zd*)gM, h->Nb, h->Ns, h->wpow,
+                                                                gd, 1.0 / P, 0.5 * M / (P * P), (zd*)g);
+  g_launches++;
+  const cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(s);
+  cudaFree(gd);
+  if (e != cudaSuccess) { set_error("gradient-source kernel launch failed"); return MARIE_ERR_CUDA; }
+  return MARIE_OK;
+}
+
+marie_status marie_vie_gradient(marie_vie* h, const void* J, const void* lam, const void* E, double M, double P,
+                                double* d_eps, double* d_sigma, void* stream) {
+  if (!h || !J || !lam || !E || !d_eps || !d_sigma || !(P > 0)) {
+    set_error("marie_vie_gradient: invalid argument");
+    return MARIE_ERR_BAD_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* gd = nullptr;
+  MARIE_TRY(upload_gdiag(h, &gd, s));
+  k_grad<<<(unsigned)((h->Ns + 255) / 256), 256, 0, s>>>((const zd*)J, (const zd*)lam, (const zd*)E, h->Ns, h->C, gd,
+                                                         h->mr_body, h->ce_im, 0.5 * M / (P * P), d_eps, d_sigma);
+  g_launches++;
+  const cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(s);
+  cudaFree(gd);
+  if (e != cudaSuccess) { set_error("gradient kernel launch failed"); return MARIE_ERR_CUDA; }
   return MARIE_OK;
 }
 

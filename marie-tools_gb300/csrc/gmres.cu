@@ -419,6 +419,7 @@ struct Scratch {
   marie_vie* h;
   std::vector<std::pair<void*, size_t>>* pool;
   size_t next = 0;
+  bool adjoint = false;   // the solve's operator is A^H (mvp_vie's Hermitian adjoint)
   explicit Scratch(marie_vie* hh) : h(hh), pool(&hh->gm_pool) {}
   Scratch(marie_vie* hh, std::vector<std::pair<void*, size_t>>* p) : h(hh), pool(p) {}
   template <typename P>
@@ -533,8 +534,8 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     for (int r = 0; r < nrhs; ++r) if (start[r]) log[r].outer = outit;
     incyc = start;
     for (int k = 0; k < m; ++k) {
-      MARIE_TRY(launch_matvec<T>(h, MV_VIE, OP_N, V + (int64_t)k * ld, vrs, V + (int64_t)(k + 1) * ld, vrs, nrhs,
-                                 st.incyc, s));
+      MARIE_TRY(launch_matvec<T>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N,
+                                 V + (int64_t)k * ld, vrs, V + (int64_t)(k + 1) * ld, vrs, nrhs, st.incyc, s));
       ++*matvecs;
       k_dots<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, st.incyc, st.part, nch);
       MARIE_LAUNCH_CHECK();
@@ -604,7 +605,8 @@ static marie_status true_residual(marie_vie* h, int nrhs, const zd* b, const zd*
   MARIE_TRY(sc.get(&npart, (size_t)nrhs * nch));
   MARIE_TRY(sc.get(&nr, nrhs));
   MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, mask.data(), nrhs, cudaMemcpyHostToDevice, s));
-  MARIE_TRY(launch_matvec<double>(h, MV_VIE, OP_N, (const cplx<double>*)x, Nb, (cplx<double>*)r, Nb, nrhs, d_mask, s));
+  MARIE_TRY(launch_matvec<double>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N,
+                                  (const cplx<double>*)x, Nb, (cplx<double>*)r, Nb, nrhs, d_mask, s));
   ++*matvecs;
   k_residual<<<vgrid(Nb, nrhs), 256, 0, s>>>(b, r, Nb, d_mask);
   MARIE_LAUNCH_CHECK();
@@ -680,6 +682,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
   const int64_t Nb = h->Nb;
   const int m = o->restart;
   Scratch sc(h);
+  sc.adjoint = o->adjoint != 0;
   std::vector<RhsLog> log(nrhs);
   std::vector<double> bnorm;
   MARIE_TRY(norms(h, nrhs, b, bnorm, s, sc));

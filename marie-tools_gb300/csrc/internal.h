@@ -84,6 +84,7 @@ struct marie_vie {
   uint16_t* zq = nullptr;            // device, 8: z_live in four-step order (n3 = 16*NB)
   int64_t* idxS = nullptr;           // device, Ns (0-based linear voxel index)
   double* wpow = nullptr;            // device, Ns: real(Mc_inv/ce) per body voxel
+  marie::cplx<double>* mr_body = nullptr;   // device, Ns: Mr per body voxel
   std::vector<int64_t> idxS_host;
   marie::BlockTab tab[4];            // N, N_adj, K, K_adj
   marie::PrecState<double> p64;

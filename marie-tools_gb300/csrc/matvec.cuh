@@ -41,6 +41,7 @@ enum MvMode : int {
   MV_VIE_ADJ = 2,   // y = x - N^H(invG .* conj(chi) .* x) on the body vector
   MV_EFIELD = 3,    // y = (1/ce) (invG(N x) - x) on the body (em_efield_vie_excitation.m:21)
   MV_HFIELD = 4,    // y = invG(K x) on the body (em_hfield_vie_excitation.m:20)
+  MV_HFIELD_ADJ = 5,  // y = K^H(invG x) on the body: the adjoint of the MV_HFIELD map
 };
 
 // Per-axis lookup tables (device pointers).
@@ -125,6 +126,8 @@ __device__ __forceinline__ void body_store(const MvArgs<T>& a, int c, int s, int
   cplx<T> r;
   if (a.mode == MV_HFIELD) {
     r = scale(v, a.invg[c]);
+  } else if (a.mode == MV_HFIELD_ADJ) {
+    r = v;
   } else {
     const cplx<T> xin = io_load<T>(a.in[(int64_t)rhs * a.in_rs + o]);
     if (a.mode == MV_VIE) r = xin - scale(a.chi[s] * v, a.invg[c]);
@@ -175,6 +178,7 @@ __global__ void k_fwd_x(MvArgs<T> a) {
         if (s >= 0) {
           v = in[(int64_t)c * a.Ns + s];
           if (a.mode == MV_VIE_ADJ) v = scale(mulc(v, a.chi[s]), a.invg[c]);
+          else if (a.mode == MV_HFIELD_ADJ) v = scale(v, a.invg[c]);
         }
       }
     }

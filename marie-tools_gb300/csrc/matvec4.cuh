@@ -132,6 +132,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_fwd_x(MvArgs<T
           if (s >= 0) {
             val = io_load<T>(in[(int64_t)c * a.Ns + s]);
             if (a.mode == MV_VIE_ADJ) val = scale(mulc(val, a.chi[s]), a.invg[c]);
+            else if (a.mode == MV_HFIELD_ADJ) val = scale(val, a.invg[c]);
           }
         }
       }

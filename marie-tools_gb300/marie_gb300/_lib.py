@@ -50,7 +50,7 @@ class VieDesc(ct.Structure):
 class GmresOpts(ct.Structure):
     _fields_ = [("restart", ct.c_int32), ("maxit", ct.c_int32), ("tol", ct.c_double), ("mode", ct.c_int32),
                 ("x0_present", ct.c_int32), ("inner_tol", ct.c_double), ("max_refine", ct.c_int32),
-                ("inner_safety", ct.c_double)]
+                ("inner_safety", ct.c_double), ("adjoint", ct.c_int32)]
 
 
 class GmresReport(ct.Structure):
@@ -87,6 +87,9 @@ _PROTOS = {
     "marie_vie_fields": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, _vp, _vp, _vp, ct.c_int32, _vp]),
     "marie_vie_absorbed_power": (ct.c_int, [_vp, _vp, ct.c_int32, c_double_p, _vp]),
     "marie_vie_b1_plus": (ct.c_int, [_vp, _vp, ct.c_int32, _vp, _vp]),
+    "marie_vie_apply_hfield_adjoint": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, _vp]),
+    "marie_vie_gradient_source": (ct.c_int, [_vp, _vp, _vp, ct.c_double, ct.c_double, _vp, _vp]),
+    "marie_vie_gradient": (ct.c_int, [_vp, _vp, _vp, _vp, ct.c_double, ct.c_double, _vp, _vp, _vp]),
     "marie_last_error": (ct.c_char_p, []),
     "marie_version": (ct.c_char_p, []),
     "marie_launch_count": (ct.c_int64, []),

@@ -228,13 +228,35 @@ class VieOperator:
                                           self._stream()))
         return out
 
+    def apply_hfield_adjoint(self, x, out=None):
+        """K^H(invG x) on body vectors: the adjoint of the H-field map."""
+        return self._apply(self._lib.marie_vie_apply_hfield_adjoint, x, self.Nb, out)
+
+    def gradient_source(self, J, gM, M, P):
+        """Adjoint source g = gM/P - (M/P^2)(1/2) D J of J_obj = M/P (one right-hand side)."""
+        import torch
+        g = torch.empty_like(J)
+        check(self._lib.marie_vie_gradient_source(self._h, ct.c_void_p(J.data_ptr()), ct.c_void_p(gM.data_ptr()),
+                                                  float(M), float(P), ct.c_void_p(g.data_ptr()), self._stream()))
+        return g
+
+    def gradient(self, J, lam, E, M, P):
+        """dJ_obj/d eps_r and dJ_obj/d sigma per body voxel (two float64 CUDA tensors of length N_s)."""
+        import torch
+        de = torch.empty(self.Ns, dtype=torch.float64, device="cuda")
+        ds = torch.empty_like(de)
+        check(self._lib.marie_vie_gradient(self._h, ct.c_void_p(J.data_ptr()), ct.c_void_p(lam.data_ptr()),
+                                           ct.c_void_p(E.data_ptr()), float(M), float(P),
+                                           ct.c_void_p(de.data_ptr()), ct.c_void_p(ds.data_ptr()), self._stream()))
+        return de, ds
+
     # -- solve ----------------------------------------------------------------
     def _run_gmres(self, fn, bptr, xptr, nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
-                   raise_on_fail, inner_safety=0.0):
+                   raise_on_fail, inner_safety=0.0, adjoint=False):
         o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol,
                            mode=SOLVE_MIXED if mode == "mixed" else SOLVE_FP64,
                            x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine,
-                           inner_safety=inner_safety)
+                           inner_safety=inner_safety, adjoint=1 if adjoint else 0)
         it = np.zeros(nrhs, np.int32); ou = np.zeros(nrhs, np.int32); li = np.zeros(nrhs, np.int32)
         tr = np.zeros(nrhs, np.float64); st = np.zeros(nrhs, np.int32); rl = np.zeros(nrhs, np.int32)
         rv = np.zeros((nrhs, resvec_cap), np.float64)
@@ -248,8 +270,9 @@ class VieOperator:
                            rep.matvecs_c128, rep.matvecs_c64, ok=(s == 0))
 
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
-              max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0):
-        """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA."""
+              max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0, adjoint=False):
+        """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA.
+        adjoint=True solves A^H x = b."""
         import torch
         b = b.contiguous()
         if b.dtype != torch.complex128 or b.device.type != "cuda":
@@ -260,7 +283,7 @@ class VieOperator:
             x = torch.zeros_like(b)
         report = self._run_gmres(self._lib.marie_gmres_vie, ct.c_void_p(b.data_ptr()), ct.c_void_p(x.data_ptr()),
                                  nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
-                                 raise_on_fail, inner_safety)
+                                 raise_on_fail, inner_safety, adjoint)
         return x, report
 
     def gmres_host(self, b, x=None, *, out=None, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,

@@ -202,3 +202,42 @@ def em_ehfield_vie(op: VieOperator, Jb, Ue, Ub):
     E, H = op.fields(J, Ue=Ut, Ub=Bt)
     phi = op.absorbed_power(J)
     return E.reshape(npt, op.Nb).t(), H.reshape(npt, op.Nb).t(), phi
+
+
+def b1_objective(op: VieOperator, J, Ue, Ub, roi):
+    """J_obj = mean_ROI |B1+|^2 / P_abs of one solved current J (complex128
+    CUDA, N_b): B1+ = mu0 (H_x + i H_y) (em_ehfield_vie.m:68), P_abs =
+    phi(1,1)/2 (em_ehfield_vie.m:44-52).  roi: body-voxel indices (0-based,
+    into idxS).  Returns (J_obj, M, P, E, H, b1)."""
+    import torch
+    E, H = op.fields(J, Ue=Ue, Ub=Ub)
+    b1 = op.b1_plus(H)
+    r = torch.as_tensor(np.asarray(roi), device="cuda")
+    M = float((b1[r].abs() ** 2).mean())
+    P = 0.5 * float(op.absorbed_power(J)[0, 0].real)
+    return M / P, M, P, E, H, b1
+
+
+def b1_objective_gradient(op: VieOperator, b, Ue, Ub, roi, *, tol=1e-6, mode="mixed", J=None):
+    """Adjoint gradient of J_obj = mean_ROI |B1+|^2 / P_abs with respect to
+    eps_r and sigma of every body voxel, for the solution J of A J = b (one
+    right-hand side; J is solved here unless given).  Steps: forward solve,
+    fields, B1+ and P; adjoint source g = dJ_obj/dconj(J) (the B1+ part
+    through marie_vie_apply_hfield_adjoint); adjoint solve A^H lam = g;
+    per-voxel sensitivities (marie_vie_gradient).  Returns (J_obj, d_eps,
+    d_sigma, J)."""
+    import torch
+    if J is None:
+        J, _rep = op.gmres(b, tol=tol, mode=mode)
+    Jobj, M, P, E, H, b1 = b1_objective(op, J, Ue, Ub, roi)
+    Ns, l = op.Ns, 4 if op.pwl else 1
+    r = torch.as_tensor(np.asarray(roi), device="cuda")
+    w = torch.zeros(op.Nb, dtype=torch.complex128, device="cuda")
+    w[r] = b1[r]
+    w[l * Ns + r] = -1j * b1[r]
+    mu0 = 4e-7 * np.pi
+    gM = op.apply_hfield_adjoint(w) * (mu0 / len(roi))
+    g = op.gradient_source(J, gM, M, P)
+    lam, _repa = op.gmres(g, tol=tol, mode=mode, adjoint=True)
+    de, ds = op.gradient(J, lam, E, M, P)
+    return Jobj, de, ds, J
