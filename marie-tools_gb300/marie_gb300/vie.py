@@ -241,3 +241,36 @@ def b1_objective_gradient(op: VieOperator, b, Ue, Ub, roi, *, tol=1e-6, mode="mi
     lam, _repa = op.gmres(g, tol=tol, mode=mode, adjoint=True)
     de, ds = op.gradient(J, lam, E, M, P)
     return Jobj, de, ds, J
+
+
+def _b1_objective_function():
+    import torch
+
+    class B1Objective(torch.autograd.Function):
+        """J_obj = mean_ROI |B1+|^2 / P_abs as a differentiable function of the
+        body voxels' eps_r and sigma (float64 tensors of length N_s).  `build`
+        (eps_r, sigma as numpy) -> (VieOperator, b, Ue, Ub) creates the
+        operator for given materials; backward uses the adjoint sensitivities
+        of b1_objective_gradient."""
+
+        @staticmethod
+        def forward(ctx, eps_r, sigma, build, roi, tol, mode):
+            op, b, Ue, Ub = build(eps_r.detach().cpu().numpy(), sigma.detach().cpu().numpy())
+            try:
+                Jobj, de, ds, _J = b1_objective_gradient(op, b, Ue, Ub, roi, tol=tol, mode=mode)
+            finally:
+                op.close()
+            ctx.save_for_backward(de.to(eps_r.device), ds.to(sigma.device))
+            return torch.tensor(Jobj, dtype=torch.float64, device=eps_r.device)
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            de, ds = ctx.saved_tensors
+            return grad_out * de, grad_out * ds, None, None, None, None
+
+    return B1Objective
+
+
+def b1_objective_autograd(eps_r, sigma, build, roi, *, tol=1e-6, mode="mixed"):
+    """torch.autograd entry point of the B1+ objective (see _b1_objective_function)."""
+    return _b1_objective_function().apply(eps_r, sigma, build, roi, tol, mode)

@@ -9,6 +9,8 @@ with respect to each body voxel's eps_r and sigma (GPU).
 * 96^3 PWL ellipsoid with a 20^3 ROI (the adjoint-gradient configuration's
   size): the gradient from mixed-precision solves against the one from
   complex128 solves, within 1e-3.
+* torch.autograd through vie.b1_objective_autograd: backward returns the
+  adjoint sensitivities, chained through a function of the materials.
 """
 import numpy as np
 import pytest
@@ -104,3 +106,42 @@ def test_b1_gradient_mixed_matches_fp64_at_96():
         a, ref = a.cpu().numpy(), ref.cpu().numpy()
         assert np.linalg.norm(a - ref) <= 1e-3 * np.linalg.norm(ref)
     op.close()
+
+
+@pytest.mark.gpu
+def test_b1_objective_autograd_wrapper():
+    """torch.autograd through vie.b1_objective_autograd returns the adjoint
+    sensitivities (and the chain rule through a function of the materials)."""
+    from marie_gb300 import assemble_green, phantoms
+    from marie_gb300 import vie
+    res, freq, pwl = 5e-3, 297.2e6, True
+    body = phantoms.sphere(16, res, 0.03, 50.0, 0.6)
+    ivN = assemble_green(body.n, res, freq, pwl, "N")
+    ivK = assemble_green(body.n, res, freq, pwl, "K")
+    loops, radius = phantoms.loop_outside((0.03, 0.03, 0.03), gap=0.01, radius=0.02)
+    roi = np.arange(0, body.idxS.size, 5)
+    cache = {}
+
+    def build(er_s, se_s):
+        er, se = body.er.copy(), body.se.copy()
+        g = np.unravel_index(body.idxS, body.n, order="F")
+        er[g], se[g] = er_s, se_s
+        b2 = phantoms.Body(body.n, body.res, body.origin, er, se, body.idxS)
+        op = _setup(b2, res, freq, pwl, 3, ivN, ivK)
+        if "Ue" not in cache:
+            cache["Ue"] = op.incident_loops(body.origin, loops, radius, nseg=64)
+        Ue = cache["Ue"]
+        return op, _rhs(op, b2, freq, pwl, Ue), Ue, torch.zeros_like(Ue)
+
+    g = np.unravel_index(body.idxS, body.n, order="F")
+    er0 = torch.tensor(body.er[g], dtype=torch.float64, device="cuda", requires_grad=True)
+    se0 = torch.tensor(body.se[g], dtype=torch.float64, device="cuda", requires_grad=True)
+    scale = torch.tensor(1.5, dtype=torch.float64, device="cuda")
+    J = vie.b1_objective_autograd(er0 * scale, se0, build, roi, tol=1e-12, mode="fp64")
+    J.backward()
+    op, b, Ue, Ub = build(body.er[g] * 1.5, body.se[g])
+    _J, de, ds, _ = vie.b1_objective_gradient(op, b, Ue, Ub, roi, tol=1e-12, mode="fp64")
+    op.close()
+    assert abs(float(J) - _J) <= 1e-12 * abs(_J)
+    assert torch.allclose(er0.grad, 1.5 * de, rtol=1e-10, atol=0)
+    assert torch.allclose(se0.grad, ds, rtol=1e-10, atol=0)
