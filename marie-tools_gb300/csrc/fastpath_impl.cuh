@@ -37,11 +37,17 @@ static void launch_y(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStre
   }
 }
 
+// complex64: the packed-pair kernel k4_zp; complex128 (native or float-float): k4_z
 template <typename T, int NB, bool PWL, int OP>
 static void launch_z4(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
   static std::atomic<uint64_t> o{0};
-  smem_opt_in(k4_z<T, NB, PWL, OP>, o);
-  k4_z<T, NB, PWL, OP><<<g, 256, smem, s>>>(a);
+  if constexpr (std::is_same<T, float>::value) {
+    smem_opt_in(k4_zp<NB, PWL, OP>, o);
+    k4_zp<NB, PWL, OP><<<g, kZpThreads, smem, s>>>(a);
+  } else {
+    smem_opt_in(k4_z<T, NB, PWL, OP>, o);
+    k4_z<T, NB, PWL, OP><<<g, 256, smem, s>>>(a);
+  }
 }
 
 template <typename T>

@@ -56,7 +56,7 @@ struct PrecState {
   cplx<T>* chi = nullptr;     // Ns
   cplx<T>* GN = nullptr;      // nblkN * oct
   cplx<T>* GK = nullptr;      // nblkK * oct
-  cplx<T>* GNf = nullptr;     // 8 n1 n2 n3 * nblkN, [ky][kx][kz][blk] (four-step grids)
+  cplx<T>* GNf = nullptr;     // 8 n1 n2 n3 * nblkN, [ky][kx][kz][blk] (four-step grids; complex64: pair layout)
   cplx<T>* T1 = nullptr;      // ws_rhs * C * n3 * n2 * 2n1
   cplx<T>* S = nullptr;       // ws_rhs * C * 2n2 * n3 * 2n1
   int ws_rhs = 0;             // right-hand sides per matvec chunk

@@ -353,3 +353,4 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
 }  // namespace marie
 
 #include "kz4.cuh"
+#include "kz4p.cuh"

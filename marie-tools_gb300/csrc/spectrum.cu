@@ -121,6 +121,30 @@ __global__ void k_full_store(const zd* tmp, cplx<T>* dst, int n1, int n2, int n3
   }
 }
 
+// The same for the complex64 z pass (k4_zp), pair layout: frequencies 2k and
+// 2k+1 of a column share one 16-byte entry (re, re, im, im) at
+// ((ky*2n1 + kx)*U + blk)*n3 + k.
+__global__ void k_full_store_pair(const zd* tmp, float* dst, int n1, int n2, int n3, int U, int blk, int s1, int s2,
+                                  int s3, double scl) {
+  const int m1 = 2 * n1, m2 = 2 * n2, m3 = 2 * n3;
+  const int nkx = n1 + 1, nky = n2 + 1;
+  const int64_t total = (int64_t)m1 * m2 * m3;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % m3);
+    const int64_t r = idx / m3;
+    const int kx = (int)(r % m1);
+    const int ky = (int)(r / m1);
+    const bool mx = kx > n1, my = ky > n2, mz = kz > n3;
+    const int kxo = mx ? m1 - kx : kx, kyo = my ? m2 - ky : ky, kzo = mz ? m3 - kz : kz;
+    const double sg = (double)((mx ? s1 : 1) * (my ? s2 : 1) * (mz ? s3 : 1)) * scl;
+    const zd v = tmp[kxo + (int64_t)nkx * (kyo + (int64_t)nky * kzo)];
+    float* d = dst + ((r * U + blk) * n3 + (kz >> 1)) * 4 + (kz & 1);
+    d[0] = (float)(v.x * sg);
+    d[2] = (float)(v.y * sg);
+  }
+}
+
 static unsigned grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 65535LL * 16) b = 65535LL * 16;
@@ -240,7 +264,8 @@ static marie_status build_op(marie_vie* h, const marie_tucker_block* tk, const d
       g_launches++;
     }
     if (dst.f32) {
-      k_full_store<float><<<grid_for(full), 256>>>(tmp, dst.f32, n1, n2, n3, nblk, id, s1, s2, s3, scl);
+      k_full_store_pair<<<grid_for(full), 256>>>(tmp, reinterpret_cast<float*>(dst.f32), n1, n2, n3, nblk, id, s1, s2,
+                                                  s3, scl);
       g_launches++;
     }
     if (dst.fff) {

@@ -182,6 +182,28 @@ def test_four_step_path(n, pwl, prec, monkeypatch):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
+@pytest.mark.parametrize("n3", [64, 80, 96, 112, 128])
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_four_step_z_lengths(n3, pwl, prec):
+    """z lengths 16*NB for NB = 4..8 (the z pass is compiled per NB): N and
+    N^H on a 16 x 16 x n3 grid against the oracle, 3 right-hand sides."""
+    n = (16, 16, n3)
+    P = _problem(n, pwl)
+    op = P.gpu_operator(max_rhs=4)
+    J = P.random_grid(seed=9, nrhs=3)
+    x = torch.from_numpy(np.concatenate([flat_F(J[r]) for r in range(3)])).to("cuda", _dt(prec))
+    for name, adj, fn in (("N", False, op.apply_N), ("N", True, op.apply_N_adj)):
+        y = fn(x).cpu().numpy().astype(np.complex128)
+        for r in range(3):
+            ref = O.mvp_op_tucker(J[r], P.TN, name, adj, cache={})
+            sl = slice(r * J[r].size, (r + 1) * J[r].size)
+            assert rel_err(unflat_F(y[sl], n, P.C), ref) <= TOL[prec], (name, adj, r)
+    op.close()
+    _CACHE.pop((n, pwl), None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
 @pytest.mark.parametrize("precisions,prec", [(3, "c128"), (3, "c64"), (6, "c128")], ids=["c128", "c64", "c128ff"])
 def test_pruned_passes_on_a_partial_body(pwl, precisions, prec, monkeypatch):
     """A body inside a sub-box leaves grid rows and z slices without body
