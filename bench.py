@@ -149,14 +149,24 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
     alg = units * per_rhs + green
     achieved = alg / (ms_z * 1e-3) / 1e9
     # ncu dram bytes (read + write) of one 16-RHS z-pass launch of this
-    # workload (profiles/k4_z_c64_128pwl_16rhs_dram.md)
+    # workload (profiles/k4_zp_c64_128pwl_16rhs_dram.md)
     traffic = ZTRAFFIC_128PWL_16RHS if (wl["pwl"] and n == 128 and units == 16) else None
     four_step = n % 16 == 0 and 16 <= n <= 128
-    name = (f"k4_z<float,{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
+    name = (f"k4_zp<{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
+    # FP32 work of the same launch: per right-hand side and (kx, ky) column,
+    # C forward + C inverse zero-padded transforms (two n-point halves each,
+    # 5 m log2 m flops per m-point transform, plus 6 flops per point for the
+    # odd half's w_2n twist) and the Green product (C*C complex multiply-adds,
+    # 8 flops each, at 2n frequencies); against the FP32 FMA rate of 152 SMs
+    # x 128 lanes x 2 flops at the SM clock sampled during the run
+    fft = 2 * C * (2 * 5 * n * math.log2(n) + 6 * n)
+    prod = 2 * n * C * C * 8
+    flops = units * (2 * n) ** 2 * (fft + prod)
     return {"kernel": name + " (z FFT + Green block multiply + inverse z FFT)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "traffic": traffic, "alg_bytes_per_launch": int(alg), "launch_ms": round(ms_z, 4),
-            "units_per_launch": units, "peak_source": peak_kind}
+            "units_per_launch": units, "peak_source": peak_kind,
+            "fp32": {"flops_per_launch": int(flops), "achieved_tflops": round(flops / (ms_z * 1e-3) / 1e12, 2)}}
 
 
 ZTRAFFIC_128PWL_16RHS = 26.14e9
@@ -256,6 +266,13 @@ def run_ours(args, wl):
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else FP64_ITERS_ELLIPSOID128), budget_s=args.cpu_budget)
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if sm_mhz:
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        fp32_peak = nsm * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof["fp32"].update({"peak_tflops": round(fp32_peak, 2), "frac": round(roof["fp32"]["achieved_tflops"] / fp32_peak, 4),
+                             "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 flops x {sm_mhz:.0f} MHz (sampled)"})
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
@@ -268,7 +285,7 @@ def run_ours(args, wl):
                        "l2": "inputs larger than L2 (Krylov basis and FFT work arrays are tens of GB)",
                        "parallelism": f"replicas x{ws} (independent RHS batches, no collective)"},
             "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clk.summary(), "roofline": roof, "cpu_baseline": cpu,
+            "clocks": clocks, "roofline": roof, "cpu_baseline": cpu,
             "solve": {"iters_per_rhs_mean": float(np.mean(rep.iters)), "matvecs_c64": int(rep.matvecs_c64),
                       "matvecs_c128": int(rep.matvecs_c128), "true_resid_max": float(np.max(rep.true_resid)),
                       "converged": int(np.sum(rep.status == 0))},
