@@ -39,37 +39,59 @@ constexpr bool blk_has_neg(int blk) {
   return false;
 }
 
-// One entry of the Green product of a frequency pair (entries sorted by
-// block; every index a compile-time constant).  y_p += sgn * g * x_q with
-// g (or conj(g) for N^H) in the lanes (G(2k), G(2k+1)):
+// The Green product of one frequency pair runs in two sweeps over the entry
+// list, outputs p < C/2 then p >= C/2 (the inputs stay in registers): half
+// the accumulators leaves registers for more Green loads in flight, at the
+// price of loading blocks that serve both halves twice.  in_half: entry K
+// writes output half H; first_in_half: no earlier entry of its block does.
+template <bool PWL, int OP>
+constexpr bool in_half(int K, int H) {
+  using Tab = OpTab<PWL, OP>;
+  constexpr int C = PWL ? 12 : 3;
+  return (Tab::L.e[K].p < C / 2) == (H == 0);
+}
+template <bool PWL, int OP>
+constexpr bool first_in_half(int K, int H) {
+  using Tab = OpTab<PWL, OP>;
+  for (int i = 0; i < K; ++i)
+    if (Tab::L.e[i].blk == Tab::L.e[K].blk && in_half<PWL, OP>(i, H)) return false;
+  return true;
+}
+
+// One entry of output half H (entries sorted by block; every index a
+// compile-time constant).  y_p += sgn * g * x_q with g (or conj(g) for N^H)
+// in the lanes (G(2k), G(2k+1)):
 //   re += gr*xr - gi*xi,  im += gr*xi + gi*xr.
-template <bool PWL, int OP, int K>
+template <bool PWL, int OP, int H, int K>
 struct ZPointP {
   static __device__ __forceinline__ void run(cp* y, const cp* x, f2& gr, f2& gi, f2& ngi, f2& ngr,
                                              const float4* gp, int gs) {
     using Tab = OpTab<PWL, OP>;
-    constexpr int blk = Tab::L.e[K].blk;
-    constexpr int p = Tab::L.e[K].p, q = Tab::L.e[K].q, sg = Tab::L.e[K].sgn;
-    constexpr bool first = (K == 0) || (Tab::L.e[K == 0 ? 0 : K - 1].blk != blk);
-    if constexpr (first) {
-      const float4 g = __ldg(gp + (int64_t)blk * gs);
-      gr = f2_make(g.x, g.y);
-      const f2 gim = f2_make(g.z, g.w);
-      if constexpr ((OP & 1) != 0) {   // conj(g)
-        ngi = gim;
-        gi = f2_neg(gim);
-      } else {
-        gi = gim;
-        ngi = f2_neg(gim);
+    if constexpr (in_half<PWL, OP>(K, H)) {
+      constexpr int blk = Tab::L.e[K].blk;
+      constexpr int p = Tab::L.e[K].p, q = Tab::L.e[K].q, sg = Tab::L.e[K].sgn;
+      constexpr int C = PWL ? 12 : 3;
+      constexpr int pp = p - (H == 0 ? 0 : C / 2);
+      if constexpr (first_in_half<PWL, OP>(K, H)) {
+        const float4 g = __ldg(gp + (int64_t)blk * gs);
+        gr = f2_make(g.x, g.y);
+        const f2 gim = f2_make(g.z, g.w);
+        if constexpr ((OP & 1) != 0) {   // conj(g)
+          ngi = gim;
+          gi = f2_neg(gim);
+        } else {
+          gi = gim;
+          ngi = f2_neg(gim);
+        }
+        if constexpr (blk_has_neg<PWL, OP>(blk)) ngr = f2_neg(gr);
       }
-      if constexpr (blk_has_neg<PWL, OP>(blk)) ngr = f2_neg(gr);
-    }
-    if constexpr (sg > 0) {
-      y[p].re = fma2(gr, x[q].re, fma2(ngi, x[q].im, y[p].re));
-      y[p].im = fma2(gr, x[q].im, fma2(gi, x[q].re, y[p].im));
-    } else {
-      y[p].re = fma2(ngr, x[q].re, fma2(gi, x[q].im, y[p].re));
-      y[p].im = fma2(ngr, x[q].im, fma2(ngi, x[q].re, y[p].im));
+      if constexpr (sg > 0) {
+        y[pp].re = fma2(gr, x[q].re, fma2(ngi, x[q].im, y[pp].re));
+        y[pp].im = fma2(gr, x[q].im, fma2(gi, x[q].re, y[pp].im));
+      } else {
+        y[pp].re = fma2(ngr, x[q].re, fma2(gi, x[q].im, y[pp].re));
+        y[pp].im = fma2(ngr, x[q].im, fma2(ngi, x[q].re, y[pp].im));
+      }
     }
   }
 };
@@ -78,22 +100,34 @@ template <bool PWL, int OP, int... Ks>
 __device__ __forceinline__ void zpoint_pair(std::integer_sequence<int, Ks...>, cp* v, int qstride, const float4* gp,
                                             int gs) {
   constexpr int C = PWL ? 12 : 3;
-  cp x[C], y[C];
+  constexpr int CH = C / 2;
+  cp x[C];
   const f2 zero = f2_make(0.f, 0.f);
 #pragma unroll
-  for (int q = 0; q < C; ++q) {
-    x[q] = lds_cp(v + q * qstride);
-    y[q] = cp{zero, zero};
-  }
+  for (int q = 0; q < C; ++q) x[q] = lds_cp(v + q * qstride);
   f2 gr = zero, gi = zero, ngi = zero, ngr = zero;
-  (ZPointP<PWL, OP, Ks>::run(y, x, gr, gi, ngi, ngr, gp, gs), ...);
+  {
+    cp y[CH];
 #pragma unroll
-  for (int p = 0; p < C; ++p) sts_cp(v + p * qstride, y[p]);
+    for (int p = 0; p < CH; ++p) y[p] = cp{zero, zero};
+    (ZPointP<PWL, OP, 0, Ks>::run(y, x, gr, gi, ngi, ngr, gp, gs), ...);
+#pragma unroll
+    for (int p = 0; p < CH; ++p) sts_cp(v + p * qstride, y[p]);
+  }
+  {
+    cp y[C - CH];
+#pragma unroll
+    for (int p = 0; p < C - CH; ++p) y[p] = cp{zero, zero};
+    (ZPointP<PWL, OP, 1, Ks>::run(y, x, gr, gi, ngi, ngr, gp, gs), ...);
+#pragma unroll
+    for (int p = 0; p < C - CH; ++p) sts_cp(v + (CH + p) * qstride, y[p]);
+  }
 }
 
 // 192 threads: at the 128^3 PWL tile (W = 4) steps 1 and B have 384 tasks,
 // steps 2 and A 768, and two CTAs per SM leave 168 registers per thread
-// (the 12 + 12 complex pairs of the Green product fit without spilling).
+// (the product's 12 input and 6 output pairs plus Green loads in flight,
+// without spilling).
 constexpr int kZpThreads = 192;
 
 template <int NB, bool PWL, int OP>
