@@ -16,13 +16,15 @@ __host__ __device__ constexpr int kz4_halfpad(int W) { return W >= 16 ? 0 : 8 / 
 // Sequence stride of k4_zp (complex64, packed pairs) in 16-byte pairs.
 __host__ __device__ constexpr int kzp_stride(int N, int W) { return N + (W >= 8 ? 1 : 8 / W); }
 
-// Shared-memory bytes of the z pass: k4_z (twiddles + both halves) or, for
-// complex64, k4_zp (twiddle tables, slice masks, pairs).
+// Shared-memory bytes of the z pass: k4_z (native complex128: twiddles +
+// both halves), k4_zf (float-float: 32-byte twiddle entries + both halves)
+// or k4_zp (complex64: twiddle tables, slice masks, pairs).
 template <typename T>
 __host__ inline size_t kz4_smem(int N, int C, int W) {
   if (sizeof(T) == 4) return (size_t)32 * N + 32 + (size_t)C * W * kzp_stride(N, W) * 16;
   const size_t half = (size_t)C * W * kz4_stride(N, W);
-  return (N + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
+  const size_t twn = std::is_same<T, ff>::value ? 2 * N : N;
+  return (twn + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
 }
 
 template <typename T>

@@ -37,13 +37,17 @@ static void launch_y(bool inv, const MvArgs<T>& a, dim3 g, size_t smem, cudaStre
   }
 }
 
-// complex64: the packed-pair kernel k4_zp; complex128 (native or float-float): k4_z
+// complex64: the packed-pair kernel k4_zp; complex128 in float-float: k4_zf
+// (packed (re, im) pairs); native complex128: k4_z
 template <typename T, int NB, bool PWL, int OP>
 static void launch_z4(const MvArgs<T>& a, dim3 g, size_t smem, cudaStream_t s) {
   static std::atomic<uint64_t> o{0};
   if constexpr (std::is_same<T, float>::value) {
     smem_opt_in(k4_zp<NB, PWL, OP>, o);
     k4_zp<NB, PWL, OP><<<g, kZpThreads, smem, s>>>(a);
+  } else if constexpr (std::is_same<T, ff>::value) {
+    smem_opt_in(k4_zf<NB, PWL, OP>, o);
+    k4_zf<NB, PWL, OP><<<g, 256, smem, s>>>(a);
   } else {
     smem_opt_in(k4_z<T, NB, PWL, OP>, o);
     k4_z<T, NB, PWL, OP><<<g, 256, smem, s>>>(a);

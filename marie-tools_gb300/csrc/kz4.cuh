@@ -1,6 +1,8 @@
 // Four-step z pass of the matvec (n3 = 16*NB): z-DFT, Green block multiply
 // and inverse z-DFT in shared memory, for W = TX*R contiguous elements of
-// every (component, z) row.
+// every (component, z) row.  k4_z serves native complex128; complex64 and
+// float-float complex128 run the packed-pair kernels of kz4p.cuh and
+// kz4f.cuh, which keep this layout and work split.
 //
 // Shared-memory layout.  Half h (0: even frequencies, 1: odd) starts at
 // h*H; in it, sequence (c, e) starts at (c*W + e)*S.  Inside a sequence the
@@ -17,7 +19,6 @@
 
 #include "fastpath.cuh"
 #include "matvec4.cuh"
-#include "pair.cuh"
 
 namespace marie {
 
@@ -81,129 +82,6 @@ __device__ __forceinline__ void zpoint(std::integer_sequence<int, Ks...>, cplx<T
   (ZPoint<T, PWL, OP, Ks>::run(y, x, gv, gnext, gp), ...);
 #pragma unroll
   for (int p = 0; p < C; ++p) v[p * qstride] = y[p];
-}
-
-// ---------------------------------------------------------------------------
-// Float-float PWL multiply of one point for N / N^H.  Unrolled like zpoint,
-// the 144 entries are thousands of instructions in float-float and overflow
-// the instruction cache, so here the output group P and the input group Q run
-// as loops (three trips each) over a body holding the ten Tucker indices j
-// unrolled: block (j, k) with k = PQ_N(P, Q) - 1, entries (l, lp) with
-// |LLP(l, lp)| = j + 1 (the same for every (P, Q) since PQ_N carries no sign).
-// The arithmetic runs in packed FP32 pairs with (re, im) in the two lanes;
-// accumulators stay unnormalised (hi, lo) pairs until the end.
-// ---------------------------------------------------------------------------
-struct PwlPQ {
-  int jl[4][4];          // Tucker index j of entry (l, lp)
-  int sg[4][4];          // its sign
-};
-
-template <int OP>
-constexpr PwlPQ make_pwl_pq() {
-  using Tab = OpTab<true, OP>;
-  PwlPQ t{};
-  for (int i = 0; i < Tab::NE; ++i) {
-    const OpEntry e = Tab::L.e[i];
-    if (e.p < 4 && e.q < 4) {      // (P, Q) = (0, 0): block (j, 0)
-      t.jl[e.p][e.q] = e.blk / 6;
-      t.sg[e.p][e.q] = e.sgn;
-    }
-  }
-  return t;
-}
-
-// Complex float-float value with (re, im) in the two lanes of packed FP32
-// pairs: hi = (re.hi, im.hi), lo = (re.lo, im.lo).
-struct ffc2 {
-  f2 hi, lo;
-};
-
-// acc += a*b per lane (NEG: acc -= a*b) on unnormalised float-float pairs:
-// product error by FMA, sum error by two-sum, both collected in acc.lo.  na
-// is -a; the error term is accumulated negated (p - a*b) so that every FMA
-// adds, which gives the same values as the scalar form a*b - p.
-template <bool NEG>
-__device__ __forceinline__ void ff_acc2(ffc2& acc, const ffc2& a, const ffc2& na, const ffc2& b) {
-  const ffc2& A = NEG ? na : a;
-  const ffc2& NA = NEG ? a : na;
-  const f2 p = A.hi * b.hi;
-  f2 e = fma2(NA.hi, b.hi, p);
-  e = fma2(NA.hi, b.lo, e);
-  e = fma2(NA.lo, b.hi, e);
-  const f2 s = acc.hi + p;
-  const f2 bb = s - acc.hi;
-  const f2 sl = (acc.hi - (s - bb)) + (p - bb);
-  acc.hi = s;
-  acc.lo = acc.lo + (sl - e);
-}
-
-// y += sgn * g * x for g = gr + i gi: lanes (re, im) += gr * (xr, xi) and
-// (re, im) += (-gi, gi) * (xi, xr), in the order of the scalar form.
-template <int OP>
-__device__ __forceinline__ void zpoint_pwl_ff(cplx<ff>* v, int qstride, const cplx<ff>* gp) {
-  constexpr PwlPQ TB = make_pwl_pq<OP>();
-  const f2 zero = f2_make(0.f, 0.f);
-  // all inputs in registers first (outputs go back in place); the output
-  // group P and the input group Q both run as loops, so the unrolled body
-  // is the ten blocks of one (P, Q) pair
-  cplx<ff> xin[12];
-#pragma unroll
-  for (int q = 0; q < 12; ++q) xin[q] = v[q * qstride];
-#pragma unroll 1
-  for (int P = 0; P < 3; ++P) {
-    ffc2 y[4];
-#pragma unroll
-    for (int l = 0; l < 4; ++l) y[l] = ffc2{zero, zero};
-#pragma unroll 1
-    for (int Q = 0; Q < 3; ++Q) {
-      ffc2 x[4], xs[4];
-#pragma unroll
-      for (int lp = 0; lp < 4; ++lp) {
-        const cplx<ff> t = Q == 0 ? xin[lp] : (Q == 1 ? xin[4 + lp] : xin[8 + lp]);
-        x[lp] = ffc2{f2_make(t.x.hi, t.y.hi), f2_make(t.x.lo, t.y.lo)};
-        xs[lp] = ffc2{f2_make(t.y.hi, t.x.hi), f2_make(t.y.lo, t.x.lo)};
-      }
-      const int k = P + Q + ((P > 0 && Q > 0) ? 1 : 0);    // PQ_N(P, Q) - 1
-      const cplx<ff>* gk = gp + k;                          // block (j, k) at 6j + k
-#pragma unroll
-      for (int j = 0; j < 10; ++j) {
-        const float4 g = __ldg(reinterpret_cast<const float4*>(gk + 6 * j));   // (gr.hi, gr.lo, gi.hi, gi.lo)
-        const ffc2 a1{f2_bc(g.x), f2_bc(g.y)};
-        const ffc2 na1{zero - a1.hi, zero - a1.lo};
-        ffc2 a2{f2_make(-g.z, g.z), f2_make(-g.w, g.w)};
-        ffc2 na2{zero - a2.hi, zero - a2.lo};
-        if constexpr ((OP & 1) != 0) {   // conj(g)
-          const ffc2 t = a2;
-          a2 = na2;
-          na2 = t;
-        }
-#pragma unroll
-        for (int l = 0; l < 4; ++l) {
-#pragma unroll
-          for (int lp = 0; lp < 4; ++lp) {
-            if (TB.jl[l][lp] == j) {
-              if (TB.sg[l][lp] > 0) {
-                ff_acc2<false>(y[l], a1, na1, x[lp]);
-                ff_acc2<false>(y[l], a2, na2, xs[lp]);
-              } else {
-                ff_acc2<true>(y[l], a1, na1, x[lp]);
-                ff_acc2<true>(y[l], a2, na2, xs[lp]);
-              }
-            }
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int l = 0; l < 4; ++l) {
-      const f2 s = y[l].hi + y[l].lo;
-      const f2 e = y[l].lo - (s - y[l].hi);
-      float sr, si, er, ei;
-      f2_split(s, sr, si);
-      f2_split(e, er, ei);
-      v[(4 * P + l) * qstride] = cplx<ff>{ff(sr, er), ff(si, ei)};
-    }
-  }
 }
 
 template <typename T, int NB, bool PWL, int OP>
@@ -286,10 +164,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
     const int kx = 2 * (kxp - alpha * n1) + alpha;
     const cplx<T>* gp = a.G + (((int64_t)ky * m1 + kx) * (2 * N) + kz) * U;
     cplx<T>* v = buf + g * H + e * S + zpos(k >> 4, k & 15);
-    if constexpr (PWL && std::is_same<T, ff>::value && OP <= 1)
-      zpoint_pwl_ff<OP>(v, W * S, gp);
-    else
-      zpoint<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, v, W * S, gp);
+    zpoint<T, PWL, OP>(std::make_integer_sequence<int, NE>{}, v, W * S, gp);
   }
   __syncthreads();
   // inverse step A (in place): task (s, k1), k1 fastest

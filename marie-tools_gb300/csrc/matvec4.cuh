@@ -77,9 +77,15 @@ __device__ __forceinline__ void dft6(cplx<T>* v) {
   }
 }
 
+// Float-float DFTs run in packed (re, im) pairs (ffpair.cuh).
+template <bool INV, int N>
+__device__ __forceinline__ void dftn_ffc2(cplx<ff>* v);
+
 template <typename T, bool INV, int N>
 __device__ __forceinline__ void dftn(cplx<T>* v) {
-  if constexpr (N == 1) {
+  if constexpr (std::is_same<T, ff>::value && N > 1) {
+    dftn_ffc2<INV, N>(v);
+  } else if constexpr (N == 1) {
   } else if constexpr (N == 6) {
     dft6<T, INV>(v);
   } else if constexpr (N == 16) {
@@ -354,3 +360,4 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k4_inv_y(MvArgs<T
 
 #include "kz4.cuh"
 #include "kz4p.cuh"
+#include "kz4f.cuh"
