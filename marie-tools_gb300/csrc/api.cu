@@ -51,6 +51,9 @@ void dev_free_all(marie_vie* h) {
   h->gm_pool.clear();
   for (auto& e : h->io_pool) cudaFree(e.first);
   h->io_pool.clear();
+  if (h->hio) cudaFreeHost(h->hio);
+  h->hio = nullptr;
+  h->hio_cap = 0;
   h->mem_used = 0;
 }
 

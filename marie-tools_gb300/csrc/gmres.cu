@@ -455,6 +455,66 @@ struct Scratch {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Status channel.  The solver's small host<->device transfers (residual norms,
+// active masks, per-rhs counters; a few hundred bytes, several per Arnoldi
+// step) go through pinned, device-mapped host memory moved by k_bytes rather
+// than through cudaMemcpyAsync: the host-buffer solve keeps the copy engines
+// busy with chunk copies, and a small copy queued behind one stalls the
+// solve for the chunk copy's duration.  Slot i of 16*nrhs bytes serves one
+// transfer; a slot is rewritten by the host only after a stream
+// synchronisation that follows the previous kernel reading it.
+// ---------------------------------------------------------------------------
+enum ChanSlot { SLOT_TOLABS, SLOT_MASK, SLOT_BETA, SLOT_INCYC, SLOT_RESID, SLOT_KR, SLOT_TODO, SLOT_NORM, kSlots };
+
+__global__ void k_bytes(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+static marie_status chan_reserve(marie_vie* h, int nrhs) {
+  const size_t need = (size_t)kSlots * 16 * std::max(nrhs, 1);
+  if (h->hio_cap >= need) return MARIE_OK;
+  if (h->hio) cudaFreeHost(h->hio);
+  h->hio = nullptr;
+  h->hio_cap = 0;
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, need, cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("pinned status buffer allocation of %zu bytes failed", need);
+    return MARIE_ERR_OOM;
+  }
+  h->hio = (unsigned char*)p;
+  h->hio_cap = need;
+  return MARIE_OK;
+}
+static unsigned char* chan_slot(marie_vie* h, int slot, int nrhs) {
+  return h->hio + (size_t)slot * 16 * std::max(nrhs, 1);
+}
+// host -> device through the slot
+static marie_status chan_put(marie_vie* h, int slot, int nrhs, void* dst, const void* src, size_t bytes,
+                             cudaStream_t s) {
+  MARIE_TRY(chan_reserve(h, nrhs));
+  unsigned char* q = chan_slot(h, slot, nrhs);
+  memcpy(q, src, bytes);
+  unsigned char* qd = nullptr;
+  MARIE_CUDA_TRY(cudaHostGetDevicePointer((void**)&qd, q, 0));
+  k_bytes<<<1, 256, 0, s>>>(qd, (unsigned char*)dst, (int)bytes);
+  MARIE_LAUNCH_CHECK();
+  return MARIE_OK;
+}
+// device -> slot (read it with chan_take after synchronising the stream)
+static marie_status chan_get(marie_vie* h, int slot, int nrhs, const void* src, size_t bytes, cudaStream_t s) {
+  MARIE_TRY(chan_reserve(h, nrhs));
+  unsigned char* qd = nullptr;
+  MARIE_CUDA_TRY(cudaHostGetDevicePointer((void**)&qd, chan_slot(h, slot, nrhs), 0));
+  k_bytes<<<1, 256, 0, s>>>((const unsigned char*)src, qd, (int)bytes);
+  MARIE_LAUNCH_CHECK();
+  return MARIE_OK;
+}
+static void chan_take(marie_vie* h, int slot, int nrhs, void* dst, size_t bytes) {
+  memcpy(dst, chan_slot(h, slot, nrhs), bytes);
+}
+
 static dim3 vgrid(int64_t Nb, int nrhs) {
   int64_t bx = (Nb + 255) / 256;
   if (bx > 4096) bx = 4096;
@@ -494,11 +554,12 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
   MARIE_TRY(sc.get(&st.npart, (size_t)nrhs * nch));
   unsigned char* d_mask = nullptr;
   MARIE_TRY(sc.get(&d_mask, nrhs));
-  MARIE_CUDA_TRY(cudaMemsetAsync(st.H, 0, sizeof(zd) * nrhs * mp1 * m, s));
+  k_zero<<<vgrid((int64_t)nrhs * mp1 * m, 1), 256, 0, s>>>(st.H, (int64_t)nrhs * mp1 * m);
+  MARIE_LAUNCH_CHECK();
   std::vector<double> tolabs(nrhs);
   for (int r = 0; r < nrhs; ++r) tolabs[r] = tolrel[r] * bnorm[r];
-  MARIE_CUDA_TRY(cudaMemcpyAsync(st.tolabs, tolabs.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, todo.data(), nrhs, cudaMemcpyHostToDevice, s));
+  MARIE_TRY(chan_put(h, SLOT_TOLABS, nrhs, st.tolabs, tolabs.data(), nrhs * sizeof(double), s));
+  MARIE_TRY(chan_put(h, SLOT_MASK, nrhs, d_mask, todo.data(), nrhs, s));
   const int64_t ld = Nb;
   const int64_t vrs = (int64_t)mp1 * Nb;
   const dim3 cg((unsigned)nch, (unsigned)nrhs);
@@ -509,8 +570,9 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
   k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
   MARIE_LAUNCH_CHECK();
   std::vector<double> beta(nrhs, 0.0);
-  MARIE_CUDA_TRY(cudaMemcpyAsync(beta.data(), st.beta, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MARIE_TRY(chan_get(h, SLOT_BETA, nrhs, st.beta, nrhs * sizeof(double), s));
   MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  chan_take(h, SLOT_BETA, nrhs, beta.data(), nrhs * sizeof(double));
   std::vector<unsigned char> start(nrhs, 0);
   int nstart = 0;
   for (int r = 0; r < nrhs; ++r) {
@@ -526,7 +588,7 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
   int outit = 0;
   while (nstart > 0) {
     ++outit;
-    MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, start.data(), nrhs, cudaMemcpyHostToDevice, s));
+    MARIE_TRY(chan_put(h, SLOT_MASK, nrhs, d_mask, start.data(), nrhs, s));
     k_scale<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, vrs, Nb, d_mask, st.beta);
     MARIE_LAUNCH_CHECK();
     k_cycle_init<<<sb, 128, 0, s>>>(st, m, nrhs, d_mask);
@@ -551,9 +613,11 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
       k_givens<<<sb, 128, 0, s>>>(st, k, m, nrhs);
       MARIE_LAUNCH_CHECK();
       prev = incyc;
-      MARIE_CUDA_TRY(cudaMemcpyAsync(incyc.data(), st.incyc, nrhs, cudaMemcpyDeviceToHost, s));
-      MARIE_CUDA_TRY(cudaMemcpyAsync(resid.data(), st.resid, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+      MARIE_TRY(chan_get(h, SLOT_INCYC, nrhs, st.incyc, nrhs, s));
+      MARIE_TRY(chan_get(h, SLOT_RESID, nrhs, st.resid, nrhs * sizeof(double), s));
       MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+      chan_take(h, SLOT_INCYC, nrhs, incyc.data(), nrhs);
+      chan_take(h, SLOT_RESID, nrhs, resid.data(), nrhs * sizeof(double));
       int any = 0;
       for (int r = 0; r < nrhs; ++r) {
         if (!prev[r]) continue;
@@ -564,8 +628,8 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
       if (!any) break;
     }
     // finalize the cycle of every rhs that ran it
-    MARIE_CUDA_TRY(cudaMemcpyAsync(kr.data(), st.kr, nrhs * sizeof(int), cudaMemcpyDeviceToHost, s));
-    MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, start.data(), nrhs, cudaMemcpyHostToDevice, s));
+    MARIE_TRY(chan_get(h, SLOT_KR, nrhs, st.kr, nrhs * sizeof(int), s));
+    MARIE_TRY(chan_put(h, SLOT_MASK, nrhs, d_mask, start.data(), nrhs, s));
     k_solve_y<<<sb, 128, 0, s>>>(st, m, nrhs, d_mask);
     MARIE_LAUNCH_CHECK();
     k_xupdate<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, ld, mp1, m, Nb, d_mask, st, x, Nb);
@@ -577,6 +641,7 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
     MARIE_LAUNCH_CHECK();
     MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+    chan_take(h, SLOT_KR, nrhs, kr.data(), nrhs * sizeof(int));
     nstart = 0;
     for (int r = 0; r < nrhs; ++r) {
       if (!start[r]) continue;
@@ -604,7 +669,7 @@ static marie_status true_residual(marie_vie* h, int nrhs, const zd* b, const zd*
   double *npart = nullptr, *nr = nullptr;
   MARIE_TRY(sc.get(&npart, (size_t)nrhs * nch));
   MARIE_TRY(sc.get(&nr, nrhs));
-  MARIE_CUDA_TRY(cudaMemcpyAsync(d_mask, mask.data(), nrhs, cudaMemcpyHostToDevice, s));
+  MARIE_TRY(chan_put(h, SLOT_NORM, nrhs, d_mask, mask.data(), nrhs, s));
   MARIE_TRY(launch_matvec<double>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N,
                                   (const cplx<double>*)x, Nb, (cplx<double>*)r, Nb, nrhs, d_mask, s));
   ++*matvecs;
@@ -615,8 +680,9 @@ static marie_status true_residual(marie_vie* h, int nrhs, const zd* b, const zd*
   k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(npart, nch, nrhs, d_mask, nr);
   MARIE_LAUNCH_CHECK();
   std::vector<double> v(nrhs);
-  MARIE_CUDA_TRY(cudaMemcpyAsync(v.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MARIE_TRY(chan_get(h, SLOT_NORM, nrhs, nr, nrhs * sizeof(double), s));
   MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  chan_take(h, SLOT_NORM, nrhs, v.data(), nrhs * sizeof(double));
   rel.resize(nrhs);
   for (int k = 0; k < nrhs; ++k)
     if (mask[k]) rel[k] = bnorm[k] > 0 ? v[k] / bnorm[k] : 0.0;
@@ -634,8 +700,9 @@ static marie_status norms(marie_vie* h, int nrhs, const zd* v, std::vector<doubl
   k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(npart, nch, nrhs, nullptr, nr);
   MARIE_LAUNCH_CHECK();
   out.resize(nrhs);
-  MARIE_CUDA_TRY(cudaMemcpyAsync(out.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
+  MARIE_TRY(chan_get(h, SLOT_NORM, nrhs, nr, nrhs * sizeof(double), s));
   MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  chan_take(h, SLOT_NORM, nrhs, out.data(), nrhs * sizeof(double));
   return MARIE_OK;
 }
 
@@ -718,7 +785,10 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
     if (o->x0_present) {
       MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, rel, &mv64, s, sc));
     } else {
-      MARIE_CUDA_TRY(cudaMemcpyAsync(r64, b, sizeof(zd) * Nb * nrhs, cudaMemcpyDeviceToDevice, s));
+      // a kernel, not a copy-engine transfer (see the status channel above)
+      k_convert<double, double><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)b, Nb, (cplx<double>*)r64, Nb, Nb,
+                                                                nullptr);
+      MARIE_LAUNCH_CHECK();
       for (int r = 0; r < nrhs; ++r) rel[r] = bnorm[r] > 0 ? 1.0 : 0.0;
     }
     const double floor_tol = o->inner_tol > 0 ? o->inner_tol : 1e-7;
@@ -736,7 +806,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
       if (n == 0) break;
       unsigned char* d_todo = nullptr;
       MARIE_TRY(sc.get(&d_todo, nrhs));
-      MARIE_CUDA_TRY(cudaMemcpyAsync(d_todo, todo.data(), nrhs, cudaMemcpyHostToDevice, s));
+      MARIE_TRY(chan_put(h, SLOT_TODO, nrhs, d_todo, todo.data(), nrhs, s));
       k_convert<double, float><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)r64, Nb, V, (int64_t)(m + 1) * Nb, Nb, d_todo);
       MARIE_LAUNCH_CHECK();
       // inner problem A d = r: relative tolerance w.r.t. ||r||, asking for just
@@ -774,10 +844,11 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
 }
 
 // Host-buffer form: b and x in host memory (pinned for overlap).  The
-// right-hand sides are solved in chunks of the matvec chunk size through two
-// device buffer pairs: chunk k+1 is copied in before chunk k is solved, and
-// chunk k is copied out on a second stream while chunk k+1 is solved, so
-// only the first copy in and the last copy out are exposed.
+// right-hand sides are solved in chunks of at most the matvec chunk size
+// through two device buffer pairs: chunk k+1 is copied in before chunk k is
+// solved, and chunk k is copied out on a second stream while chunk k+1 is
+// solved, so only the first copy in and the last copy out are exposed, and
+// those two chunks are made small.
 extern "C" marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, void* x_host, int32_t nrhs,
                                              const marie_gmres_opts* o, marie_gmres_report* rep, void* stream) {
   if (!h || !b_host || !x_host || !o) { set_error("NULL argument"); return MARIE_ERR_BAD_ARG; }
@@ -789,7 +860,24 @@ extern "C" marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, v
     if (atoi(e) > 0) cs = atoi(e);
   }
   cs = std::max(1, std::min(cs, (int)nrhs));
-  const int nch = (nrhs + cs - 1) / cs;
+  // chunk schedule: only the first copy in and the last copy out are
+  // exposed, so the first and last chunks are a quarter chunk and the rest
+  // full chunks (64 = 4 + 16 + 16 + 16 + 8 + 4 for chunks of 16)
+  std::vector<int> c0, cn;
+  {
+    const int q = std::max(1, cs / 4);
+    int left = nrhs, r0 = 0;
+    auto add = [&](int n) { c0.push_back(r0); cn.push_back(n); r0 += n; left -= n; };
+    if (nrhs > 2 * q + cs) {
+      add(q);
+      while (left > cs + q) add(cs);
+      if (left > q) add(left - q);
+      add(left);
+    } else {
+      while (left > 0) add(std::min(cs, left));
+    }
+  }
+  const int nch = (int)c0.size();
   cudaStream_t s = (cudaStream_t)stream;
   Scratch sc(h, &h->io_pool);
   zd *bd[2] = {nullptr, nullptr}, *xd[2] = {nullptr, nullptr};
@@ -812,7 +900,7 @@ extern "C" marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, v
   const zd* bh = (const zd*)b_host;
   zd* xh = (zd*)x_host;
   auto copy_in = [&](int k) -> marie_status {
-    const int r0 = k * cs, nk = std::min(cs, nrhs - r0), u = k & 1;
+    const int r0 = c0[k], nk = cn[k], u = k & 1;
     const size_t bytes = sizeof(zd) * (size_t)nk * Nb;
     if (cudaMemcpyAsync(bd[u], bh + (int64_t)r0 * Nb, bytes, cudaMemcpyHostToDevice, cps) != cudaSuccess ||
         (o->x0_present && cudaMemcpyAsync(xd[u], xh + (int64_t)r0 * Nb, bytes, cudaMemcpyHostToDevice, cps) != cudaSuccess)) {
@@ -826,7 +914,7 @@ extern "C" marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, v
   if (st != MARIE_OK) return finish(st);
   int worst = MARIE_OK, mv64 = 0, mv32 = 0;
   for (int k = 0; k < nch; ++k) {
-    const int r0 = k * cs, nk = std::min(cs, nrhs - r0), u = k & 1;
+    const int r0 = c0[k], nk = cn[k], u = k & 1;
     if (k + 1 < nch && (st = copy_in(k + 1)) != MARIE_OK) return finish(st);
     cudaStreamWaitEvent(s, ev_in[u], 0);
     marie_gmres_report sub = {};

@@ -96,6 +96,11 @@ struct marie_vie {
   // frees them; destroy frees everything).
   std::vector<std::pair<void*, size_t>> gm_pool;
   std::vector<std::pair<void*, size_t>> io_pool;   // device buffers of the host-buffer solve
+  // Pinned, device-mapped host memory for the solver's per-iteration status
+  // (residuals, masks): moved by a kernel, so it never queues on a copy
+  // engine behind the chunk copies of the host-buffer solve.
+  unsigned char* hio = nullptr;
+  size_t hio_cap = 0;
 };
 
 namespace marie {
