@@ -160,10 +160,11 @@ marie_status marie_gmres_vie(marie_vie* h, const void* b, void* x, int32_t nrhs,
 
 /* marie_gmres_vie with b and x in host memory (nrhs x N_b complex128; x
  * holds x0 on entry when opts->x0_present).  The right-hand sides are solved
- * in chunks of the matvec chunk size; copies of the next chunk in and the
- * previous chunk out run on a second stream while a chunk is solved, so with
- * page-locked host buffers only the first copy in and the last copy out are
- * exposed.  The MATLAB host-array path of is_gmres_vie (to_GPU.m:8-51). */
+ * in chunks of at most the matvec chunk size; copies of the next chunk in and
+ * the previous chunk out run on a second stream while a chunk is solved, so
+ * with page-locked host buffers only the first copy in and the last copy out
+ * are exposed, and the first and last chunks are a quarter chunk.  The MATLAB
+ * host-array path of is_gmres_vie (to_GPU.m:8-51). */
 marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, void* x_host, int32_t nrhs,
                                   const marie_gmres_opts* opts, marie_gmres_report* report, void* stream);
 
