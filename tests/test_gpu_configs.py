@@ -10,6 +10,9 @@
   (float-float operator) both reach 1e-6 true residual and agree within
   1e-5 (the field-error target), and the solution satisfies A x = b to the
   reported residual when re-applied through the complex128 operator.
+* The PWC sweep: sixteen seeded phantoms with edges drawn from
+  {48, 64, 80, 96, 112, 128} at 2 mm, f in {128, 297.2} MHz, 1-8 loops each,
+  bodies scaled to the grid: mixed and complex128 solves of every loop.
 """
 import numpy as np
 import pytest
@@ -106,3 +109,38 @@ def test_pwc_phantoms_various_edges(n, freq):
     assert repm.ok and repf.ok and repm.true_resid[0] <= 1e-6 and repf.true_resid[0] <= 1e-6
     assert rel_err(xm.cpu().numpy(), xf.cpu().numpy()) <= 1e-5
     op.close()
+
+
+@pytest.mark.gpu
+def test_pwc_sweep_sixteen_phantoms():
+    """Sixteen seeded PWC phantoms (edges from {48, ..., 128}, 2 mm, 128 or
+    297.2 MHz, 1-8 loops on a ring around the body, bodies scaled to the
+    grid): for every loop the mixed solve and the complex128 solve
+    (float-float operator) reach 1e-6 true residual and agree within 1e-5."""
+    from marie_gb300 import VieOperator, assemble_green, phantoms
+    rng = np.random.default_rng(44)
+    res = 2e-3
+    for i in range(16):
+        n = int(rng.choice([48, 64, 80, 96, 112, 128]))
+        freq = float(rng.choice([128e6, 297.2e6]))
+        nl = int(rng.integers(1, 9))
+        scale = 0.9 * (n * res / 2) / 0.090
+        body = phantoms.ellipsoid_phantom(n, res, seed=100 + i, scale=scale)
+        iv = assemble_green(body.n, res, freq, False, "N")
+        op = VieOperator(body.n, res, freq, body.idx_solution(False), body.Mr(freq), iv, pwl=False,
+                         precisions=2 | 4, max_rhs=nl)
+        del iv
+        loops = phantoms.loop_ring(nl, ring_radius=0.080 * scale + 0.01, z_extent=0.0, n_angles=nl, seed=200 + i)
+        Ue = op.incident_loops(body.origin, loops, 0.25 * n * res / 2, nseg=64).reshape(nl, -1)
+        emc = O.em_constants(freq)
+        Mr = body.Mr(freq).reshape(-1, order="F")[body.idxS]
+        chi = np.tile((1.0 / Mr) * (Mr - 1.0), 3)
+        b = (emc["ce"] * torch.from_numpy(chi).cuda()[None, :] * Ue).reshape(-1).contiguous()
+        xm, repm = op.gmres(b, restart=50, tol=1e-6, mode="mixed")
+        xf, repf = op.gmres(b, restart=50, tol=1e-6, mode="fp64")
+        assert repm.ok and repf.ok, (i, n, freq, nl)
+        assert np.max(repm.true_resid) <= 1e-6 and np.max(repf.true_resid) <= 1e-6, (i, n)
+        xm, xf = xm.cpu().numpy().reshape(nl, -1), xf.cpu().numpy().reshape(nl, -1)
+        for r in range(nl):
+            assert rel_err(xm[r], xf[r]) <= 1e-5, (i, n, freq, r)
+        op.close()
