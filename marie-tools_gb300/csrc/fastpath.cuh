@@ -15,6 +15,11 @@ __host__ __device__ constexpr int kz4_halfpad(int W) { return W >= 16 ? 0 : 8 / 
 
 // Sequence stride of k4_zp (complex64, packed pairs) in 16-byte pairs.
 __host__ __device__ constexpr int kzp_stride(int N, int W) { return N + (W >= 8 ? 1 : 8 / W); }
+// k4_zf (float-float, 16-byte elements): the same stride and an odd-half pad
+// of 4/W, which put the eight lanes of every quarter-warp of its five phases
+// on distinct 16-byte bank groups (checked by enumerating lane addresses).
+__host__ __device__ constexpr int kzf_stride(int N, int W) { return N + (W >= 8 ? 1 : 8 / W); }
+__host__ __device__ constexpr int kzf_halfpad(int W) { return W >= 8 ? 0 : 4 / W; }
 
 // Shared-memory bytes of the z pass: k4_z (native complex128: twiddles +
 // both halves), k4_zf (float-float: 32-byte twiddle entries + both halves)
@@ -22,9 +27,9 @@ __host__ __device__ constexpr int kzp_stride(int N, int W) { return N + (W >= 8 
 template <typename T>
 __host__ inline size_t kz4_smem(int N, int C, int W) {
   if (sizeof(T) == 4) return (size_t)32 * N + 32 + (size_t)C * W * kzp_stride(N, W) * 16;
+  if (std::is_same<T, ff>::value) return (2 * N + 2 * (size_t)C * W * kzf_stride(N, W) + kzf_halfpad(W)) * 16;
   const size_t half = (size_t)C * W * kz4_stride(N, W);
-  const size_t twn = std::is_same<T, ff>::value ? 2 * N : N;
-  return (twn + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
+  return (N + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
 }
 
 template <typename T>

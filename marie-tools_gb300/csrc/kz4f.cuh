@@ -1,9 +1,10 @@
 // Four-step z pass of the complex128 operator in float-float arithmetic
 // (n3 = 16*NB), every complex value in packed FP32 pairs with (re, im) in the
-// two lanes (ffpair.cuh).  Same work split, shared-memory layout and half
-// combine as k4_z (kz4.cuh); shared memory holds ffc2 values (re.hi, im.hi,
-// re.lo, im.lo), so the z-DFTs, the four-step twiddles and the Green product
-// issue one f32x2 instruction for both parts of every float-float operation.
+// two lanes (ffpair.cuh).  Same work split, half layout and half combine as
+// k4_z (kz4.cuh), with the stride and pad of 16-byte elements (kzf_stride);
+// shared memory holds ffc2 values (re.hi, im.hi, re.lo, im.lo), so the
+// z-DFTs, the four-step twiddles and the Green product issue one f32x2
+// instruction for both parts of every float-float operation.
 #pragma once
 
 #include "fastpath.cuh"
@@ -183,8 +184,8 @@ __global__ void __launch_bounds__(256, 2) k4_zf(MvArgs<ff> a) {
   const int n1 = a.n1, n2 = a.n2, m1 = 2 * n1, R = a.R;
   const int W = a.TX * R, wl = min(a.TX, m1 - k0) * R;
   const int lgW = 31 - __clz(W);                // W = TX*R is a power of two
-  const int S = kz4_stride(N, W);
-  const int H = C * W * S + kz4_halfpad(W);   // start of the odd half
+  const int S = kzf_stride(N, W);
+  const int H = C * W * S + kzf_halfpad(W);   // start of the odd half
   const int T1 = 2 * C * NB * W;              // tasks of forward step 1 / inverse step B
   fftw* tw = reinterpret_cast<fftw*>(smem_raw);
   ffc2* buf = reinterpret_cast<ffc2*>(tw + N);
