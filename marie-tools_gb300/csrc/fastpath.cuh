@@ -26,8 +26,9 @@ __host__ __device__ constexpr int kzf_halfpad(int W) { return W >= 8 ? 0 : 4 / W
 // or k4_zp (complex64: twiddle tables, slice masks, pairs).
 template <typename T>
 __host__ inline size_t kz4_smem(int N, int C, int W) {
-  if (sizeof(T) == 4) return (size_t)32 * N + 32 + (size_t)C * W * kzp_stride(N, W) * 16;
-  if (std::is_same<T, ff>::value) return (2 * N + 2 * (size_t)C * W * kzf_stride(N, W) + kzf_halfpad(W)) * 16;
+  const size_t NB = N / 16;
+  if (sizeof(T) == 4) return 560 * NB + 32 + (size_t)C * W * kzp_stride(N, W) * 16;
+  if (std::is_same<T, ff>::value) return (36 * NB + 2 * (size_t)C * W * kzf_stride(N, W) + kzf_halfpad(W)) * 16;
   const size_t half = (size_t)C * W * kz4_stride(N, W);
   return (N + 2 * half + kz4_halfpad(W)) * sizeof(cplx<T>);
 }

@@ -187,9 +187,21 @@ __global__ void __launch_bounds__(256, 2) k4_zf(MvArgs<ff> a) {
   const int S = kzf_stride(N, W);
   const int H = C * W * S + kzf_halfpad(W);   // start of the odd half
   const int T1 = 2 * C * NB * W;              // tasks of forward step 1 / inverse step B
-  fftw* tw = reinterpret_cast<fftw*>(smem_raw);
-  ffc2* buf = reinterpret_cast<ffc2*>(tw + N);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = fftw_make(a.az.tw[i]);
+  // four-step twiddles w_N^(b*k1) at b*18 + k1, high and low halves of the
+  // 32-byte entries in separate 16-byte arrays
+  ulonglong2* twh = reinterpret_cast<ulonglong2*>(smem_raw);
+  ulonglong2* twl = twh + 18 * NB;
+  ffc2* buf = reinterpret_cast<ffc2*>(twl + 18 * NB);
+  for (int i = threadIdx.x; i < 18 * NB; i += blockDim.x) {
+    const int b = i / 18, k1 = i - 18 * (i / 18);
+    const fftw t = fftw_make(k1 < 16 ? a.az.tw[b * k1] : cplx<ff>{ff(0), ff(0)});
+    twh[i] = make_ulonglong2(t.rh.v, t.ih.v);
+    twl[i] = make_ulonglong2(t.rl.v, t.il.v);
+  }
+  auto twf = [&](int i) {
+    const ulonglong2 h = twh[i], l = twl[i];
+    return fftw{f2{h.x}, f2{h.y}, f2{l.x}, f2{l.y}};
+  };
   __syncthreads();
   const int64_t row = (int64_t)m1 * R;
   const int64_t cstride = (int64_t)2 * n2 * N * row;
@@ -215,7 +227,7 @@ __global__ void __launch_bounds__(256, 2) k4_zf(MvArgs<ff> a) {
     ffc2* d = buf + h * H + (c * W + e) * S + b * 16;
     sts_ffc2(d + b, u[0]);
 #pragma unroll
-    for (int k1 = 1; k1 < 16; ++k1) sts_ffc2(d + (k1 ^ b), tw_mulf<false>(u[k1], tw[b * k1]));
+    for (int k1 = 1; k1 < 16; ++k1) sts_ffc2(d + (k1 ^ b), tw_mulf<false>(u[k1], twf(b * 18 + k1)));
   }
   __syncthreads();
   // forward step 2 (in place): task (s, k1), k1 fastest; NB-point DFT
@@ -262,7 +274,7 @@ __global__ void __launch_bounds__(256, 2) k4_zf(MvArgs<ff> a) {
     dftf<true, NB>(w);
     sts_ffc2(p + zpos(0, k1), w[0]);
 #pragma unroll
-    for (int b = 1; b < NB; ++b) sts_ffc2(p + zpos(b, k1), tw_mulf<true>(w[b], tw[b * k1]));
+    for (int b = 1; b < NB; ++b) sts_ffc2(p + zpos(b, k1), tw_mulf<true>(w[b], twf(b * 18 + k1)));
   }
   __syncthreads();
   // inverse step B: task (e, h, b, c) as in step 1, inverse 16-point DFT of

@@ -147,16 +147,21 @@ __global__ void __launch_bounds__(kZpThreads, 2) k4_zp(MvArgs<float> a) {
   const int lgW = 31 - __clz(W);                // W = TX*R is a power of two
   const int S = kzp_stride(N, W);
   const int T1 = C * NB * W;                    // tasks of forward step 1 / inverse step B
-  // twiddles: w_N^k as (wr, wr, wi, wi) and (-wi, -wi); w_2N^z; live-slice masks
+  // four-step twiddles w_N^(b*k1) at b*18 + k1 (runs of k1 contiguous,
+  // consecutive b on different bank groups) as (wr, wr, wi, wi) and
+  // (-wi, -wi); w_2N^z; live-slice masks
   ulonglong2* twq = reinterpret_cast<ulonglong2*>(smem_raw);
-  unsigned long long* twn = reinterpret_cast<unsigned long long*>(twq + N);
-  float2* tw2s = reinterpret_cast<float2*>(twn + N);
+  unsigned long long* twn = reinterpret_cast<unsigned long long*>(twq + 18 * NB);
+  float2* tw2s = reinterpret_cast<float2*>(twn + 18 * NB);
   unsigned* zqs = reinterpret_cast<unsigned*>(tw2s + N);
   cp* buf = reinterpret_cast<cp*>(zqs + 8);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const cplx<float> w = a.az.tw[i];
+  for (int i = threadIdx.x; i < 18 * NB; i += blockDim.x) {
+    const int b = i / 18, k1 = i - 18 * (i / 18);
+    const cplx<float> w = k1 < 16 ? a.az.tw[b * k1] : cplx<float>{0.f, 0.f};
     twq[i] = make_ulonglong2(f2_bc(w.x).v, f2_bc(w.y).v);
     twn[i] = f2_bc(-w.y).v;
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const cplx<float> t2 = a.az.tw2[i];
     tw2s[i] = make_float2(t2.x, t2.y);
   }
@@ -187,8 +192,8 @@ __global__ void __launch_bounds__(kZpThreads, 2) k4_zp(MvArgs<float> a) {
     sts_cp(d + b, u[0]);
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) {
-      const ulonglong2 w = twq[b * k1];
-      sts_cp(d + (k1 ^ b), tw_mul(u[k1], f2{w.x}, f2{w.y}, f2{twn[b * k1]}));
+      const ulonglong2 w = twq[b * 18 + k1];
+      sts_cp(d + (k1 ^ b), tw_mul(u[k1], f2{w.x}, f2{w.y}, f2{twn[b * 18 + k1]}));
     }
   }
   __syncthreads();
@@ -231,8 +236,8 @@ __global__ void __launch_bounds__(kZpThreads, 2) k4_zp(MvArgs<float> a) {
     sts_cp(p + zpos(0, k1), w[0]);
 #pragma unroll
     for (int b = 1; b < NB; ++b) {
-      const ulonglong2 q = twq[b * k1];
-      sts_cp(p + zpos(b, k1), tw_mulc(w[b], f2{q.x}, f2{q.y}, f2{twn[b * k1]}));
+      const ulonglong2 q = twq[b * 18 + k1];
+      sts_cp(p + zpos(b, k1), tw_mulc(w[b], f2{q.x}, f2{q.y}, f2{twn[b * 18 + k1]}));
     }
   }
   __syncthreads();
