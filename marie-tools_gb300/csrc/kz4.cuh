@@ -24,9 +24,6 @@ namespace marie {
 
 __device__ __forceinline__ int zpos(int j, int k1) { return j * 16 + (k1 ^ j); }
 
-__device__ __forceinline__ cplx<float> shfl_xor_c(cplx<float> v, int m) {
-  return {__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
-}
 __device__ __forceinline__ cplx<double> shfl_xor_c(cplx<double> v, int m) {
   return {__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
 }
@@ -38,28 +35,16 @@ __device__ __forceinline__ cplx<ff> shfl_xor_c(cplx<ff> v, int m) {
 // One entry of the single-point Green multiply (entries sorted by block;
 // every index a compile-time constant).  gp points at the point's U block
 // values, contiguous in the full spectrum ([ky][kx][kz][blk], mirror signs
-// applied), so block blk sits at the constant offset blk.  complex64 loads
-// two blocks per 16-byte load.
+// applied), so block blk sits at the constant offset blk.
 template <typename T, bool PWL, int OP, int K>
 struct ZPoint {
-  static __device__ __forceinline__ void run(cplx<T>* y, const cplx<T>* x, cplx<T>& gv, cplx<T>& gnext,
-                                             const cplx<T>* gp) {
+  static __device__ __forceinline__ void run(cplx<T>* y, const cplx<T>* x, cplx<T>& gv, const cplx<T>* gp) {
     using Tab = OpTab<PWL, OP>;
     constexpr int blk = Tab::L.e[K].blk;
     constexpr int p = Tab::L.e[K].p, q = Tab::L.e[K].q, sg = Tab::L.e[K].sgn;
     constexpr bool first = (K == 0) || (Tab::L.e[K == 0 ? 0 : K - 1].blk != blk);
-    constexpr bool pair = sizeof(T) == 4 && (Tab::L.nblk % 2) == 0;
     if constexpr (first) {
-      cplx<T> g;
-      if constexpr (pair && blk % 2 == 0) {
-        const float4 v = __ldg(reinterpret_cast<const float4*>(gp + blk));
-        g = cplx<T>{v.x, v.y};
-        gnext = cplx<T>{v.z, v.w};
-      } else if constexpr (pair) {
-        g = gnext;
-      } else {
-        g = ldg_c(gp + blk);
-      }
+      cplx<T> g = ldg_c(gp + blk);
       if constexpr ((OP & 1) != 0) g = conjg(g);
       gv = g;
     }
@@ -78,14 +63,14 @@ __device__ __forceinline__ void zpoint(std::integer_sequence<int, Ks...>, cplx<T
     x[q] = v[q * qstride];
     y[q] = cplx<T>{0, 0};
   }
-  cplx<T> gv = {0, 0}, gnext = {0, 0};
-  (ZPoint<T, PWL, OP, Ks>::run(y, x, gv, gnext, gp), ...);
+  cplx<T> gv = {0, 0};
+  (ZPoint<T, PWL, OP, Ks>::run(y, x, gv, gp), ...);
 #pragma unroll
   for (int p = 0; p < C; ++p) v[p * qstride] = y[p];
 }
 
 template <typename T, int NB, bool PWL, int OP>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::value) ? 2 : 1) k4_z(MvArgs<T> a) {
+__global__ void __launch_bounds__(256, 1) k4_z(MvArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int N = 16 * NB;
   constexpr int C = PWL ? 12 : 3;
@@ -101,9 +86,6 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   const int S = kz4_stride(N, W);
   const int H = C * W * S + kz4_halfpad(W);   // start of the odd half
   const int T1 = 2 * C * NB * W;              // tasks of forward step 1 / inverse step B
-  // two tasks' loads in flight per thread for complex64; float-float keeps
-  // one (its larger code already strains the instruction cache)
-  constexpr int kTaskUnroll = std::is_same<T, float>::value ? 2 : 1;
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + N;
   load_tw(tw, a.az.tw, N);
@@ -115,7 +97,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // forward step 1: task (e, h, b, c), e fastest; half h of the zero-padded
   // 2N-point transform (h = 1: inputs times w_2N^z), 16-point DFT over a of
   // z = NB*a + b, then the four-step twiddle.
-#pragma unroll kTaskUnroll
+#pragma unroll 1
   for (int t = threadIdx.x; t < T1; t += blockDim.x) {
     const int e = t & (W - 1), r = t >> lgW;
     const int h = r & 1, r2 = r >> 1;
@@ -188,7 +170,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 || std::is_same<T, ff>::v
   // group (tasks come in aligned groups of 2W, so t & (2W - 1) keeps (e, h)
   // and pairs partners again) and store nothing.
   const int lane = threadIdx.x & 31;
-#pragma unroll kTaskUnroll
+#pragma unroll 1
   for (int tb = threadIdx.x - lane; tb < T1; tb += blockDim.x) {
     const int t = tb + lane;
     const bool act = t < T1;
