@@ -109,11 +109,15 @@ def test_nonfinite_rhs_is_rejected():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("chunk", [None, "1", "2", "3"], ids=["default", "c1", "c2", "c3"])
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
-def test_host_buffer_solve_equals_device_solve(mode):
+def test_host_buffer_solve_equals_device_solve(mode, chunk, monkeypatch):
     """marie_gmres_vie_host (chunked, copies overlapped) returns the device
     solve's result for every right-hand side, with and without x0, and with
-    more right-hand sides than one chunk."""
+    more right-hand sides than one chunk; MARIE_HOST_CHUNK 1-3 gives the
+    uneven schedules (7 right-hand sides in chunks of 3: 1 + 3 + 2 + 1)."""
+    if chunk is not None:
+        monkeypatch.setenv("MARIE_HOST_CHUNK", chunk)
     op, A, mv, dims, emc, ep = _case("pwl_4")
     rng = np.random.default_rng(5)
     nrhs = 7
