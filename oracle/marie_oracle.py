@@ -485,6 +485,59 @@ def b1_plus(Ub, dims, mu0):
     return mu0 * (Ub[:ns] + 1j * Ub[l * ns:l * ns + ns])
 
 
+def b1_objective(J, Ue, Ub, dims, T_N, T_K, Mc, ce, roi, mu0, cache=None):
+    """J_obj = mean_ROI |B1+|^2 / P_abs for one solved current J: E and H by
+    em_efield/em_hfield_vie_excitation, B1+ = mu0 (Hx + i Hy)
+    (em_ehfield_vie.m:68), P_abs = phi(1,1)/2 (em_ehfield_vie.m:44-52).
+    roi: body-voxel indices.  Returns (J_obj, M, P, E, H, b1)."""
+    E = em_efield_vie_excitation(J, Ue, dims, T_N, ce, cache)
+    H = em_hfield_vie_excitation(J, Ub, dims, T_K, cache)
+    b1 = b1_plus(H, dims, mu0)
+    M = float(np.mean(np.abs(b1[roi]) ** 2))
+    P = 0.5 * float(np.real(em_noise_covariance(J[:, None], Mc, ce, dims)[0, 0]))
+    return M / P, M, P, E, H, b1
+
+
+def hfield_map_adjoint(w, dims, T_K, cache=None):
+    """Adjoint of J -> gather(invG K scatter(J)) (the scattered-field part of
+    em_hfield_vie_excitation.m:16-22): w -> gather(K^H invG scatter(w)),
+    invG being real and diagonal and gather the transpose of scatter."""
+    pwl = dims["ql"] == 12
+    wp = invG_scale(pwl, dims["res"])[None, None, None, :] * scatter(w, dims)
+    return gather(mvp_op_tucker(wp, T_K, "K", True, cache), dims)
+
+
+def b1_objective_gradient(J, E, b1, M, P, Mr, Mc, ce, dims, T_K, roi, mu0, solve_adjoint, cache=None):
+    """dJ_obj/d eps_r and dJ_obj/d sigma per body voxel by one adjoint solve
+    (no counterpart in the reference).  With chi = 1 - 1/Mr, A = I - chi
+    invG N on the body and b = ce chi Ue, A dJ = dchi (ce E + J) per voxel;
+    g = dJ_obj/dconj(J) = gM/P - (M/P^2)(1/2) D J with gM the ROI term
+    through the adjoint H map and D = G real(1/(Mc ce)); A^H lam = g
+    (solve_adjoint); then
+      dJ/dp_s = 2 Re(sum_c conj(lam) (ce E + J) (dMr/dp) / Mr^2)
+              + (M/P^2)(1/2) sum_c |J|^2 G_c Re((dMr/dp) / (Mc^2 ce)),
+    dMr/d eps_r = 1, dMr/d sigma = 1/ce.  Returns (d_eps, d_sigma, lam)."""
+    pwl = dims["ql"] == 12
+    ns, ql, l = dims["N_scat"], dims["ql"], dims["l"]
+    idx = dims["idxS"]
+    mr = np.asarray(Mr).reshape(-1, order="F")[idx]
+    mc = np.asarray(Mc).reshape(-1, order="F")[idx]
+    w = np.zeros(ns * ql, dtype=complex)
+    w[roi] = b1[roi]
+    w[l * ns + np.asarray(roi)] = -1j * b1[roi]
+    gM = hfield_map_adjoint(w, dims, T_K, cache) * (mu0 / len(roi))
+    gc = np.repeat(G_scale(pwl, dims["res"]), ns)
+    wpow = np.tile(np.real(1.0 / (mc * ce)), ql)
+    g = gM / P - 0.5 * (M / P ** 2) * gc * wpow * J
+    lam = solve_adjoint(g)
+    q = np.sum((np.conj(lam) * (ce * E + J)).reshape(ql, ns), axis=0)
+    jj = np.sum((np.abs(J) ** 2 * gc).reshape(ql, ns), axis=0)
+    expl = 0.5 * M / P ** 2
+    d_eps = 2 * np.real(q / mr ** 2) + expl * jj * np.real(1.0 / (mc ** 2 * ce))
+    d_sig = 2 * np.real(q / mr ** 2 / ce) + expl * jj * np.real(1.0 / (mc ** 2 * ce) / ce)
+    return d_eps, d_sig, lam
+
+
 # ---------------------------------------------------------------------------
 # GMRES
 # ---------------------------------------------------------------------------
