@@ -58,7 +58,7 @@ def time_iteration(n: int, pwl: bool, steps: int = 1, warmup: int = 0, budget_s:
         for c in range(C):
             Jp[c * n ** 3 + idxS] = xb[c * Ns:(c + 1) * Ns]
         Jp = Jp.reshape((n, n, n, C), order="F")
-        fJ = [sfft.fftn(Jp[..., q], s=(m, m, m), workers=cores).reshape(-1) for q in range(C)]
+        fJ = [sfft.fftn(Jp[..., q], s=(m, m, m), axes=(0, 1, 2), workers=cores).reshape(-1) for q in range(C)]
         out = np.empty_like(Jp)
         acc = np.empty(M, complex)
         for p in range(C):

@@ -371,7 +371,7 @@ def mvp_op_tucker(Jin: np.ndarray, T: dict, op: str = "N", adjoint: bool = False
     pwl = C == 12
     G0 = next(iter(T.values()))
     m1, m2, m3 = G0[1].shape[1], G0[2].shape[1], G0[3].shape[1]
-    fJ = [np.fft.fftn(Jin[..., i], s=(m1, m2, m3)) for i in range(C)]
+    fJ = [np.fft.fftn(Jin[..., i], s=(m1, m2, m3), axes=(0, 1, 2)) for i in range(C)]
     tab = block_table(op, pwl, adjoint)
     Jout = np.zeros_like(Jin, dtype=complex)
     for p in range(C):
