@@ -82,7 +82,15 @@ typedef struct {
 /* Build an operator handle: uploads the body map, contrast and Green's-tensor
  * spectra and sizes the workspaces.  Replaces the operator set-up of
  * ie_solver_vie.m:14 (fN = to_GPU(MREDM.operators.N,1)) together with the
- * per-product Tucker re-expansion of mvp_N_pwl_tucker.m:31 (done once here). */
+ * per-product Tucker re-expansion of mvp_N_pwl_tucker.m:31 (done once here).
+ * Any grid edge up to 1024 is accepted, as MATLAB's fftn accepts any length:
+ * a grid with an edge whose prime factors exceed 31 (e.g. 73) is embedded in
+ * a larger grid the FFT passes cover (all edges rounded up to multiples of 16
+ * when every edge is <= 128, else that edge to the next 31-smooth length),
+ * with the operator zero-padded, which leaves mvp_vie, the solves and the
+ * field maps on the caller's body unchanged; the full-grid operators below
+ * then return MARIE_ERR_NOT_SUPPORTED.  Environment MARIE_EMBED=1 embeds
+ * smooth grids with edges <= 128 the same way (four-step passes). */
 marie_status marie_vie_create(marie_vie** h, const marie_vie_desc* d);
 marie_status marie_vie_destroy(marie_vie* h);
 
@@ -92,7 +100,7 @@ marie_status marie_vie_apply(marie_vie* h, int32_t prec, const void* x, void* y,
 /* y = A^H x for A = mvp_vie: y = x - N^H(invG .* conj(Mc./Mr) .* x), with N^H
  * from mvp_N_herm_adj_{pwc,pwl}_tucker.m. */
 marie_status marie_vie_apply_adjoint(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);
-/* Raw operators on full grids (nrhs x n1*n2*n3*C):
+/* Raw operators on full grids (nrhs x n1*n2*n3*C; not on embedded grids):
  * mvp_N_{pwc,pwl}_tucker.m:1-33/43, mvp_N_herm_adj_{pwc,pwl}_tucker.m,
  * mvp_K_{pwc,pwl}_tucker.m:1-36/45, mvp_K_herm_adj_{pwc,pwl}_tucker.m. */
 marie_status marie_vie_apply_N(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, void* stream);

@@ -8,6 +8,7 @@
 #include <new>
 
 #include "fastpath.cuh"
+#include "embed.h"
 #include "internal.h"
 
 namespace marie {
@@ -502,9 +503,9 @@ static marie_status validate_desc(const marie_vie_desc* d, std::vector<int64_t>&
   return MARIE_OK;
 }
 
-extern "C" {
-
-marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
+// Handle for a grid the FFT passes take as given (marie_vie_create decides
+// whether the caller's grid is first embedded in a larger one, embed.h).
+static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
   if (!out) { set_error("output handle pointer is NULL"); return MARIE_ERR_BAD_ARG; }
   *out = nullptr;
   std::vector<int64_t> idxS;
@@ -658,6 +659,35 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   return MARIE_OK;
 }
 
+extern "C" {
+
+marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
+  if (!out) { set_error("output handle pointer is NULL"); return MARIE_ERR_BAD_ARG; }
+  *out = nullptr;
+  if (!d) { set_error("desc is NULL"); return MARIE_ERR_BAD_ARG; }
+  const int n[3] = {d->n1, d->n2, d->n3};
+  int m[3] = {d->n1, d->n2, d->n3};
+  const bool in_range = n[0] >= 1 && n[1] >= 1 && n[2] >= 1 && n[0] <= kMaxAxis && n[1] <= kMaxAxis &&
+                        n[2] <= kMaxAxis;
+  // MARIE_EMBED=1: embed every grid with edges <= 128 in the four-step grid
+  // (edges rounded up to 16*NB) even where the generic passes would run it
+  if (!in_range || !embed::embed_dims(n, env_int("MARIE_EMBED", 0) != 0, m)) return create_grid(out, d);
+  // Validate the caller's descriptor on the caller's grid; the float-float
+  // edge rule applies to the embedded grid and is checked there.
+  marie_vie_desc dv = *d;
+  if ((dv.precisions & 4) && !(dv.precisions & 1)) dv.precisions = (dv.precisions & ~4) | 2;
+  std::vector<int64_t> idxS;
+  MARIE_TRY(validate_desc(&dv, idxS));
+  embed::Buffers buf;
+  marie_vie_desc e;
+  embed::embed_desc(d, m, buf, &e);
+  MARIE_TRY(create_grid(out, &e));
+  (*out)->on1 = n[0];
+  (*out)->on2 = n[1];
+  (*out)->on3 = n[2];
+  return MARIE_OK;
+}
+
 marie_status marie_vie_release_workspace(marie_vie* h) {
   if (!h) { set_error("handle is NULL"); return MARIE_ERR_BAD_ARG; }
   cudaDeviceSynchronize();
@@ -684,6 +714,12 @@ static marie_status apply_common(marie_vie* h, int32_t prec, const void* x, void
   if (!x || !y) { set_error("x or y is NULL"); return MARIE_ERR_BAD_ARG; }
   if (nrhs < 1) { set_error("nrhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
   if (prec != MARIE_C128 && prec != MARIE_C64) { set_error("prec must be MARIE_C128 or MARIE_C64"); return MARIE_ERR_BAD_ARG; }
+  if (mode == MV_GRID && h->on1) {
+    set_error("operators on full grids are not available on this handle: its %d x %d x %d grid was embedded in "
+              "%d x %d x %d (an edge has a prime factor above 31, or MARIE_EMBED was set); body-vector "
+              "operators, solves and fields are", h->on1, h->on2, h->on3, h->n1, h->n2, h->n3);
+    return MARIE_ERR_NOT_SUPPORTED;
+  }
   const int64_t len = mode == MV_GRID ? (int64_t)h->C * h->n1 * h->n2 * h->n3 : h->Nb;
   cudaStream_t s = (cudaStream_t)stream;
   if (prec == MARIE_C128)

@@ -67,6 +67,7 @@ struct PrecState {
 
 struct marie_vie {
   int n1 = 0, n2 = 0, n3 = 0, C = 0, pwl = 0;
+  int on1 = 0, on2 = 0, on3 = 0;     // caller's grid when it was embedded in n1 x n2 x n3 (embed.h); 0 otherwise
   double res = 0, freq = 0, k0 = 0, omega = 0;
   double ce_im = 0;                  // ce = i*ce_im = i*omega*eps0
   int64_t Ns = 0, Nb = 0;

@@ -1,0 +1,19 @@
+// C entry points over the host-only grid-embedding helpers of the library
+// (marie-tools_gb300/csrc/embed.h), compiled by tests/test_embed_host.py with
+// g++ so that the helpers are checked on the CPU against numpy.
+#include "../marie-tools_gb300/csrc/embed.h"
+
+extern "C" {
+int shim_embed_dims(const int* n, int force, int* m) { return marie::embed::embed_dims(n, force != 0, m) ? 1 : 0; }
+void shim_embed_factor(const double* U, int r, int n, int m, double* out) {
+  std::vector<double> o;
+  marie::embed::embed_factor(U, r, n, m, o);
+  std::memcpy(out, o.data(), o.size() * sizeof(double));
+}
+void shim_pad_grid(const double* src, const int* n, const int* m, long long nblk, double fill, double* out) {
+  std::vector<double> o;
+  marie::embed::pad_grid(src, n, m, nblk, fill, o);
+  std::memcpy(out, o.data(), o.size() * sizeof(double));
+}
+long long shim_remap(long long lin, const int* n, const int* m) { return marie::embed::remap_voxel(lin, n, m); }
+}
