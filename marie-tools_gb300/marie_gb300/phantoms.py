@@ -61,6 +61,35 @@ def _finish(n, res, origin, er, se, mask):
     return Body(tuple(int(v) for v in n), res, origin, er, se, idxS)
 
 
+def load_rhbm(path) -> Body:
+    """A body file in MARIE's RHBM format (the reference's
+    data/bodies/.../*.mat: struct RHBM with fields r (n1 x n2 x n3 x 3 voxel
+    centres), epsilon_r, sigma_e (n1 x n2 x n3) and idxS (1-based body voxel
+    indices)), read as geo_body_domain.m:5-14 and em_assembly.m:10-12 read
+    it: grid edges from size(r), res = |r(2,1,1,1) - r(1,1,1,1)|, the body
+    from idxS (made 0-based), materials as stored.  MATLAB v5 .mat files
+    (scipy.io); a v7.3 (HDF5) file raises ValueError."""
+    import scipy.io as sio
+    try:
+        S = sio.loadmat(str(path), squeeze_me=False)
+    except NotImplementedError as e:     # v7.3 files
+        raise ValueError(f"{path}: MATLAB v7.3 (HDF5) body files are not supported; save with -v7") from e
+    if "RHBM" not in S:
+        raise ValueError(f"{path}: no RHBM struct")
+    R = S["RHBM"][0, 0]
+    r = np.asarray(R["r"], dtype=np.float64)
+    if r.ndim != 4 or r.shape[3] != 3:
+        raise ValueError(f"{path}: RHBM.r has shape {r.shape}, expected n1 x n2 x n3 x 3")
+    n = tuple(int(v) for v in r.shape[:3])
+    res = abs(r[1, 0, 0, 0] - r[0, 0, 0, 0]) if n[0] > 1 else abs(r[0, 1, 0, 1] - r[0, 0, 0, 1])
+    er = np.asarray(R["epsilon_r"], dtype=np.float64).reshape(n)
+    se = np.asarray(R["sigma_e"], dtype=np.float64).reshape(n)
+    idxS = np.asarray(R["idxS"], dtype=np.int64).reshape(-1) - 1
+    if idxS.size and (idxS.min() < 0 or idxS.max() >= int(np.prod(n))):
+        raise ValueError(f"{path}: RHBM.idxS outside the {n} grid")
+    return Body(n, float(res), r[0, 0, 0, :].copy(), er, se, idxS)
+
+
 def sphere(n=32, res=5e-3, radius=0.06, er=50.0, se=0.6) -> Body:
     """Homogeneous dielectric sphere centred in an n^3 grid."""
     nn = (n, n, n) if np.isscalar(n) else tuple(n)
