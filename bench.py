@@ -36,11 +36,11 @@ sys.path[:0] = [str(ROOT), str(ROOT / "marie-tools_gb300")]
 
 WORKLOADS = {
     "ellipsoid128": dict(n=128, res=2e-3, freq=297.2e6, pwl=True, nrhs=64, tol=1e-6, phantom="ellipsoid",
-                 desc="ellipsoid phantom 128^3 @ 2 mm, PWL, 297.2 MHz, 64 loop-port RHS"),
+                 fp64_iters=13.0, desc="ellipsoid phantom 128^3 @ 2 mm, PWL, 297.2 MHz, 64 loop-port RHS"),
     "ellipsoid96": dict(n=96, res=2e-3, freq=297.2e6, pwl=True, nrhs=1, tol=1e-6, phantom="ellipsoid",
-                 desc="ellipsoid phantom 96^3 @ 2 mm, PWL, 297.2 MHz, 1 loop RHS"),
+                 fp64_iters=13.0, desc="ellipsoid phantom 96^3 @ 2 mm, PWL, 297.2 MHz, 1 loop RHS"),
     "sphere32": dict(n=32, res=5e-3, freq=128e6, pwl=False, nrhs=1, tol=1e-6, phantom="sphere",
-                 desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
+                 fp64_iters=9.0, desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
 }
 METRIC = "GMRES solves/s at 128^3 PWL, 1e-6 resid (mixed c64/FP64-refined, 64-RHS batch)"
 
@@ -55,11 +55,10 @@ def metric_of(wl):
             f"{wl['nrhs']}-RHS batch)")
 
 
-# Mean FP64 GMRES(50) iterations per right-hand side to 1e-6 on the ellipsoid128
-# workload, measured by this library's complex128 solver (same algorithm as
-# is_gmres_vie.m); used to turn the reference arm's per-iteration time into
-# solves/s.  Updated from the 'fp64_iters_per_solve' field of our own arm.
-FP64_ITERS_ELLIPSOID128 = 13.0
+# fp64_iters (per workload above): FP64 GMRES(50) iterations per right-hand
+# side to 1e-6, measured by this library's complex128 solver (the algorithm
+# of is_gmres_vie.m; the 'iters' of our arm's 'fp64_gpu' field); they turn
+# the reference arm's per-iteration time into solves/s.
 
 
 def _dist():
@@ -282,7 +281,7 @@ def run_ours(args, wl):
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else FP64_ITERS_ELLIPSOID128), budget_s=args.cpu_budget)
+        cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else wl["fp64_iters"]), budget_s=args.cpu_budget)
     clocks = clk.summary()
     sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
     if sm_mhz:
@@ -332,7 +331,7 @@ def run_reference(args, wl):
     ws, rank, local = _dist()
     if rank != 0:
         return
-    cpu = cpu_baseline(wl, iters=FP64_ITERS_ELLIPSOID128, budget_s=1e9, steps=args.steps, warmup=args.warmup)
+    cpu = cpu_baseline(wl, iters=wl["fp64_iters"], budget_s=1e9, steps=args.steps, warmup=args.warmup)
     line = {"impl": "reference", "metric": metric_of(wl), "value": cpu["value"], "unit": "solves/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic",
