@@ -32,3 +32,21 @@ def test_uneven_batch_instances():
     assert all(d["n"] in (48, 64, 80, 96, 112, 128) and 1 <= d["nloops"] <= 8 for d in inst)
     assert {d["freq"] for d in inst} <= {128e6, 297.2e6}
     assert inst == bench.uneven_instances()           # seeded
+
+
+def test_solve_alg_bytes_formula():
+    """One iteration, no residual: one matvec of 26 n^3 C s bytes plus the
+    Green spectrum over the chunk, and Arnoldi step 1 (6 N_b s bytes); the
+    128^3 PWL complex64 matvec is 5.234 GB + 1.030 GB of Green spectrum."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    n, Nb = 128, 2939712
+    one = bench.solve_alg_bytes(n, True, Nb, [1], 0, 1)
+    assert abs(one - (26 * n ** 3 * 12 * 8 + 60 * (n + 1) ** 3 * 8 + 6 * Nb * 8)) < 1.0
+    assert abs(26 * n ** 3 * 12 * 8 / 1e9 - 5.234) < 1e-3 and abs(60 * (n + 1) ** 3 * 8 / 1e9 - 1.030) < 1e-3
+    # k = 1..13 in one cycle: sum (2k + 4) = 234; restart 5: cycles 5 + 5 + 3
+    assert abs(bench.solve_alg_bytes(n, True, Nb, [13], 0, 1) - 13 * (one - 6 * Nb * 8) - 234 * Nb * 8) < 1.0
+    assert abs(bench.solve_alg_bytes(n, True, Nb, [13], 0, 1, restart=5)
+               - 13 * (one - 6 * Nb * 8) - (2 * 50 + 24) * Nb * 8) < 1.0
+    # a complex128 residual matvec moves twice the complex64 bytes
+    assert abs(bench.solve_alg_bytes(n, True, Nb, [0], 1, 1) - 2 * (one - 6 * Nb * 8)) < 1.0
