@@ -41,7 +41,6 @@ struct NaPtrs {
   cplx<float>* tw = nullptr;
   int* maps = nullptr;
 };
-constexpr int kMaxDevices = 64;
 std::mutex g_na_mu;
 NaPtrs g_na[kMaxDevices];
 
