@@ -187,6 +187,17 @@ marie_status marie_vie_release_workspace(marie_vie* h);
  * (n1,n2,n3,pwx,6|3) interleaved complex.  kernel: 0 = N, 1 = K. */
 marie_status marie_assemble_green(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
                                   int32_t basis, int32_t kernel, double* out_host);
+
+/* marie_assemble_green with options.  flags: MARIE_GREEN_SELF_POINT_TERM adds
+ * to the self offset I_V(0,0,0) of N the point term of its kernel, (2/3)
+ * Gram_ll' on the xx, yy, zz components (Gram = diag(res^3, res^3/12 x 3)):
+ * the six N components are those of curl curl (g I), whose distributional
+ * part (2/3) delta_pq delta(r) the surface-surface near zone of assembly_N.m
+ * (:56-81) contains and the stand-in cubature does not.  Without it the
+ * field inside a quasi-static dielectric sphere comes out ~3x too small. */
+#define MARIE_GREEN_SELF_POINT_TERM 1
+marie_status marie_assemble_green_ex(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
+                                     int32_t basis, int32_t kernel, int32_t flags, double* out_host);
 /* Incident field of closed loops with unit current, tested onto the PWC/PWL
  * basis (coef_l = int E.f_l / int f_l^2): the loop/wire RHS generator.
  * loops: host, nloop x 6 doubles (centre xyz, normal xyz); out: device

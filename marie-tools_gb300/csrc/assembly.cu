@@ -4,6 +4,7 @@
 //    G_N.m:3-19, G_K.m:3-13);
 //  - incident fields of unit-current closed loops and of a plane wave, tested
 //    onto the PWC/PWL basis (the loop right-hand sides).
+#include "green_host.h"
 #include <cmath>
 #include <vector>
 
@@ -287,6 +288,18 @@ __global__ void k_plane(const int64_t* idxS, int64_t Ns, int n1, int n2, double 
 }  // namespace marie
 
 using namespace marie;
+
+extern "C" marie_status marie_assemble_green_ex(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
+                                                int32_t basis, int32_t kernel, int32_t flags, double* out_host) {
+  if (flags & ~MARIE_GREEN_SELF_POINT_TERM) {
+    set_error("marie_assemble_green_ex: unknown flags 0x%x", (unsigned)flags);
+    return MARIE_ERR_BAD_ARG;
+  }
+  const marie_status st = marie_assemble_green(n1, n2, n3, res, freq, basis, kernel, out_host);
+  if (st == MARIE_OK && (flags & MARIE_GREEN_SELF_POINT_TERM) && kernel == 0)
+    green_host::add_self_point_term(out_host, (int64_t)n1 * n2 * n3, basis == MARIE_PWL ? 10 : 1, res);
+  return st;
+}
 
 extern "C" marie_status marie_assemble_green(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
                                              int32_t basis, int32_t kernel, double* out_host) {

@@ -76,6 +76,8 @@ _PROTOS = {
                                         ct.POINTER(GmresReport), _vp]),
     "marie_assemble_green": (ct.c_int, [ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double,
                                         ct.c_int32, ct.c_int32, c_double_p]),
+    "marie_assemble_green_ex": (ct.c_int, [ct.c_int32, ct.c_int32, ct.c_int32, ct.c_double, ct.c_double,
+                                           ct.c_int32, ct.c_int32, ct.c_int32, c_double_p]),
     "marie_incident_loops": (ct.c_int, [_vp, c_double_p, c_double_p, ct.c_int32, ct.c_double,
                                         ct.c_int32, _vp, _vp]),
     "marie_incident_plane_wave": (ct.c_int, [_vp, c_double_p, _vp, _vp]),

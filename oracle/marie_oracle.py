@@ -173,13 +173,37 @@ def near_zone_standin(k0, res, pwx, kernel, offsets):
     return out
 
 
+def self_delta_term(res, pwx):
+    """The point term of the N kernel at the self offset, (pwx, 6).
+
+    The six N components are those of curl curl (g I) (G_N.m: -Gyy-Gzz, Gxy,
+    ...).  As distributions, d_p d_q g = PV(d_p d_q g) - (1/3) delta_pq
+    delta(r) and lap g = -k0^2 g - delta(r), so curl curl (g I) = PV[pointwise
+    kernel] + (2/3) delta_pq delta(r).  Integrated against T_l(r) B_l'(r') over
+    one voxel pair the point term gives (2/3) delta_pq int_V T_l B_l' =
+    (2/3) Gram_ll' on the diagonal components (xx, yy, zz: k = 0, 3, 5), with
+    Gram = diag(res^3, res^3/12, res^3/12, res^3/12) for the moments
+    [1, x/res, y/res, z/res] (the diagonal of mvp_G_pwl.m:5).  The
+    reference's surface-surface near zone (assembly_N.m:56-81) contains it;
+    a pointwise cubature of the volume kernel does not.
+    """
+    gram = np.array([res ** 3, res ** 3 / 12, res ** 3 / 12, res ** 3 / 12])
+    out = np.zeros((pwx, 6), dtype=complex)
+    for llp in range(pwx):
+        if IND_L[llp] == IND_LP[llp]:
+            out[llp, [0, 3, 5]] = (2.0 / 3.0) * gram[IND_L[llp]]
+    return out
+
+
 def assembly_op(n1, n2, n3, res, k0, pwl: bool, kernel: str = "N",
-                Np_far=4, Np_medium=8):
+                Np_far=4, Np_medium=8, self_term: str = "pointwise"):
     """Restates src/src_integral_equations/src_vie/src_operators_vie/
     assembly_N.m:16-81 and assembly_K.m:16-81 (far, medium, near zones).
 
     Returns I_V with shape (n1, n2, n3, pwx, 6) for N, (..., 3) for K.
-    The near zone uses :func:`near_zone_standin`.
+    The near zone uses :func:`near_zone_standin`; self_term="distributional"
+    adds the point term of the N kernel at the self offset
+    (:func:`self_delta_term`; K has none).
     """
     pwx = 10 if pwl else 1
     ncomp = 6 if kernel == "N" else 3
@@ -206,6 +230,10 @@ def assembly_op(n1, n2, n3, res, k0, pwl: bool, kernel: str = "N",
     nz = near_zone_standin(k0, res, pwx, kernel, near)
     for m, v in nz.items():
         I_V[m] = v
+    if self_term == "distributional" and kernel == "N":
+        I_V[0, 0, 0] += self_delta_term(res, pwx)
+    elif self_term not in ("pointwise", "distributional"):
+        raise ValueError(f"self_term must be 'pointwise' or 'distributional', got {self_term!r}")
     return I_V
 
 

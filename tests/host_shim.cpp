@@ -1,7 +1,10 @@
-// C entry points over the host-only grid-embedding helpers of the library
-// (marie-tools_gb300/csrc/embed.h), compiled by tests/test_embed_host.py with
-// g++ so that the helpers are checked on the CPU against numpy.
+// C entry points over the host-only helpers of the library (grid embedding,
+// marie-tools_gb300/csrc/embed.h; the Green's-tensor self point term,
+// marie-tools_gb300/csrc/green_host.h), compiled with g++ by the CPU tests
+// (tests/test_embed_host.py, tests/test_green_host.py) so that the helpers
+// are checked against numpy and the oracle.
 #include "../marie-tools_gb300/csrc/embed.h"
+#include "../marie-tools_gb300/csrc/green_host.h"
 
 extern "C" {
 int shim_embed_dims(const int* n, int force, int* m) { return marie::embed::embed_dims(n, force != 0, m) ? 1 : 0; }
@@ -14,6 +17,9 @@ void shim_pad_grid(const double* src, const int* n, const int* m, long long nblk
   std::vector<double> o;
   marie::embed::pad_grid(src, n, m, nblk, fill, o);
   std::memcpy(out, o.data(), o.size() * sizeof(double));
+}
+void shim_add_self_point_term(double* out, long long nD, int pwx, double res) {
+  marie::green_host::add_self_point_term(out, nD, pwx, res);
 }
 long long shim_remap(long long lin, const int* n, const int* m) { return marie::embed::remap_voxel(lin, n, m); }
 }

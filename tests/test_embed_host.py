@@ -31,8 +31,8 @@ def shim(tmp_path_factory):
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("g++ not available")
-    so = tmp_path_factory.mktemp("embed") / "libembed_shim.so"
-    subprocess.run([gxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", str(so), str(HERE / "embed_shim.cpp")],
+    so = tmp_path_factory.mktemp("embed") / "libhost_shim.so"
+    subprocess.run([gxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", str(so), str(HERE / "host_shim.cpp")],
                    check=True)
     lib = ct.CDLL(str(so))
     lib.shim_embed_factor.argtypes = [D, ct.c_int, ct.c_int, ct.c_int, D]

@@ -1,0 +1,51 @@
+"""The point term of the N kernel at the self offset on the GPU assembly
+(marie_assemble_green_ex with MARIE_GREEN_SELF_POINT_TERM, through the
+Python assemble_green(self_term="distributional")).
+
+* It adds exactly the oracle's self_delta_term to I_V(0,0,0) of N and
+  leaves every other entry, and K, as marie_assemble_green computes them.
+* Known answer: the GPU-assembled operator with it reproduces the internal
+  field 3/(eps_r + 2) E0 of a quasi-static dielectric sphere (12^3 grid,
+  1 cm voxels, r = 5 cm, 1 MHz) within the voxelisation error.
+"""
+import numpy as np
+import pytest
+
+from oracle import marie_oracle as O
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
+def test_self_point_term_flag(pwl):
+    from marie_gb300 import assemble_green
+    n, res, freq = (6, 5, 4), 2e-3, 297.2e6
+    a = assemble_green(n, res, freq, pwl, "N")
+    b = assemble_green(n, res, freq, pwl, "N", self_term="distributional")
+    want = np.zeros_like(a)
+    want[0, 0, 0] = O.self_delta_term(res, 10 if pwl else 1)
+    assert np.allclose(b - a, want, rtol=0, atol=1e-12 * np.abs(a).max())
+    k0 = assemble_green(n, res, freq, pwl, "K")
+    k1 = assemble_green(n, res, freq, pwl, "K", self_term="distributional")
+    assert np.allclose(k1, k0, rtol=0, atol=1e-12 * np.abs(k0).max())
+
+
+@pytest.mark.gpu
+def test_quasi_static_sphere_field_gpu():
+    from marie_gb300 import VieOperator, assemble_green, phantoms
+    res, freq, er = 1e-2, 1e6, 50.0
+    body = phantoms.sphere(12, res, 0.05, er, 0.0)
+    emc = O.em_constants(freq)
+    iv = assemble_green(body.n, res, freq, False, "N", self_term="distributional")
+    Mr = body.Mr(freq)
+    op = VieOperator(body.n, res, freq, body.idx_solution(False), Mr, iv, pwl=False, precisions=3, max_rhs=1)
+    Ns = body.idxS.size
+    Ue = np.concatenate([np.ones(Ns), np.zeros(Ns), np.zeros(Ns)]).astype(complex)
+    b = O.vie_rhs(emc["ce"], Mr, Mr - 1, body.idxS, 3, Ue)
+    x, rep = op.gmres(torch.from_numpy(b).cuda(), restart=50, tol=1e-8, maxit=200, mode="fp64")
+    assert rep.ok
+    Mcb = Mr.reshape(-1, order="F")[body.idxS] - 1
+    Ex = (x.cpu().numpy()[:Ns] / (emc["ce"] * Mcb)).real
+    assert abs(Ex.mean() / (3.0 / (er + 2.0)) - 1.0) < 0.15, Ex.mean()
+    op.close()
