@@ -196,6 +196,13 @@ marie_status marie_assemble_green(int32_t n1, int32_t n2, int32_t n3, double res
  * (:56-81) contains and the stand-in cubature does not.  Without it the
  * field inside a quasi-static dielectric sphere comes out ~3x too small. */
 #define MARIE_GREEN_SELF_POINT_TERM 1
+/* MARIE_GREEN_NEAR_EXACT replaces the near offsets {0,1}^3 (N or K) with an
+ * accurate host cubature of the same integrals (relative coordinate
+ * u = r - r', the box split so that u = 0 is a corner of its pieces, Duffy
+ * pyramids there, the static N singularity as a principal value over the
+ * cube plus the point term above; converged to ~1e-14), instead of the
+ * staggered 8^3 x 7^3 stand-in, which is off by 13% on face neighbours. */
+#define MARIE_GREEN_NEAR_EXACT 2
 marie_status marie_assemble_green_ex(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
                                      int32_t basis, int32_t kernel, int32_t flags, double* out_host);
 /* Incident field of closed loops with unit current, tested onto the PWC/PWL

@@ -291,14 +291,20 @@ using namespace marie;
 
 extern "C" marie_status marie_assemble_green_ex(int32_t n1, int32_t n2, int32_t n3, double res, double freq,
                                                 int32_t basis, int32_t kernel, int32_t flags, double* out_host) {
-  if (flags & ~MARIE_GREEN_SELF_POINT_TERM) {
+  if (flags & ~(MARIE_GREEN_SELF_POINT_TERM | MARIE_GREEN_NEAR_EXACT)) {
     set_error("marie_assemble_green_ex: unknown flags 0x%x", (unsigned)flags);
     return MARIE_ERR_BAD_ARG;
   }
   const marie_status st = marie_assemble_green(n1, n2, n3, res, freq, basis, kernel, out_host);
-  if (st == MARIE_OK && (flags & MARIE_GREEN_SELF_POINT_TERM) && kernel == 0)
-    green_host::add_self_point_term(out_host, (int64_t)n1 * n2 * n3, basis == MARIE_PWL ? 10 : 1, res);
-  return st;
+  if (st != MARIE_OK) return st;
+  const int pwx = basis == MARIE_PWL ? 10 : 1;
+  if (flags & MARIE_GREEN_NEAR_EXACT) {
+    const double k0 = 2 * M_PI / (299792458.0 / freq);
+    green_host::near_zone_exact(out_host, n1, n2, n3, res, k0, pwx, kernel == 0);
+  } else if ((flags & MARIE_GREEN_SELF_POINT_TERM) && kernel == 0) {
+    green_host::add_self_point_term(out_host, (int64_t)n1 * n2 * n3, pwx, res);
+  }
+  return MARIE_OK;
 }
 
 extern "C" marie_status marie_assemble_green(int32_t n1, int32_t n2, int32_t n3, double res, double freq,

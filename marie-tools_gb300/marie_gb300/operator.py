@@ -326,23 +326,27 @@ class VieOperator:
         return out
 
 
-def assemble_green(dims, res, freq, pwl: bool, kernel: str = "N", self_term: str = "pointwise") -> np.ndarray:
+def assemble_green(dims, res, freq, pwl: bool, kernel: str = "N", self_term: str = "pointwise",
+                   near: str = "standin") -> np.ndarray:
     """I_V (n1,n2,n3,pwx,6|3) computed on the GPU (assembly_N.m / assembly_K.m).
 
+    near="relative" replaces the near offsets {0,1}^3 with an accurate host
+    cubature of the same integrals (point term of N included); with
+    near="standin" (the staggered cubature of the GPU kernel),
     self_term="distributional" adds the point term of the N kernel at the
     self offset ((2/3) Gram on the diagonal components; the reference's
-    surface-surface near zone contains it, the near-zone cubature here does
-    not); "pointwise" leaves the cubature's value."""
-    if self_term not in ("pointwise", "distributional"):
-        raise ValueError(f"self_term must be 'pointwise' or 'distributional', got {self_term!r}")
+    surface-surface near zone contains it, the stand-in does not)."""
+    if self_term not in ("pointwise", "distributional") or near not in ("standin", "relative"):
+        raise ValueError(f"bad self_term {self_term!r} or near {near!r}")
     lib = _lib.load()
     n1, n2, n3 = (int(v) for v in dims)
     pwx = 10 if pwl else 1
     nc = 6 if kernel == "N" else 3
     out = np.empty(n1 * n2 * n3 * pwx * nc * 2, dtype=np.float64)
     args = (n1, n2, n3, float(res), float(freq), PWL if pwl else PWC, 0 if kernel == "N" else 1)
-    if self_term == "distributional":
-        check(lib.marie_assemble_green_ex(*args, 1, _dptr(out)))    # MARIE_GREEN_SELF_POINT_TERM
+    flags = (2 if near == "relative" else 0) | (1 if self_term == "distributional" else 0)   # MARIE_GREEN_*
+    if flags:
+        check(lib.marie_assemble_green_ex(*args, flags, _dptr(out)))
     else:
         check(lib.marie_assemble_green(*args, _dptr(out)))
     return out.view(np.complex128).reshape((n1, n2, n3, pwx, nc), order="F")

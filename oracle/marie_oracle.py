@@ -195,16 +195,114 @@ def self_delta_term(res, pwx):
     return out
 
 
+def _moment_overlap(u, m_d, res, l_axis, lp_axis):
+    """w_d(u) = int T-factor(u + x' - m_d res) B-factor(x') dx' over the
+    source-voxel interval x' in [-res/2, res/2] whose image u + x' lies in
+    the observation voxel [m_d res - res/2, m_d res + res/2]; the factors are
+    s/res on the moment's own axis and 1 otherwise (moments [1, x/res, y/res,
+    z/res], VV_Nop.m:18-19).  Exact for the quadratic integrand."""
+    lo = np.maximum(-res / 2, m_d * res - res / 2 - u)
+    hi = np.minimum(res / 2, m_d * res + res / 2 - u)
+    hi = np.maximum(hi, lo)
+    a, b = (1.0, 0.0) if not l_axis else ((u - m_d * res) / res, 1.0 / res)     # t(x') = a + b x'
+    c, d = (1.0, 0.0) if not lp_axis else (0.0, 1.0 / res)                    # b(x') = c + d x'
+    A, B, C = a * c, a * d + b * c, b * d
+    return A * (hi - lo) + B * (hi ** 2 - lo ** 2) / 2 + C * (hi ** 3 - lo ** 3) / 3
+
+
+def _moment_weights(U, m, res, pwx):
+    """W_llp(u) = int_{V_0 and V_m - u} T_l(u + r' - c_m) B_l'(r') dr' for the
+    pwx moment pairs (IND_L, IND_LP): a product of per-axis overlaps."""
+    out = np.ones((U.shape[0], pwx))
+    for llp in range(pwx):
+        l, lp = IND_L[llp], IND_LP[llp]
+        for d in range(3):
+            out[:, llp] *= _moment_overlap(U[:, d], m[d], res, l == d + 1, lp == d + 1)
+    return out
+
+
+def near_zone_relative(k0, res, pwx, kernel, offsets, order=16):
+    """I_V of the near offsets (the quantity of assembly_N.m:56-81 /
+    assembly_K.m:56-81) by an independent cubature, not the reference's
+    surface-surface/DIRECTFN route.
+
+    With u = r - r', I(m) = int K(u) W(u) du over the box prod_d [(m_d-1) res,
+    (m_d+1) res], W the moment overlap of :func:`_moment_weights` (piecewise
+    polynomial, kinks at u_d = m_d res).  The box is split at the kinks and at
+    0 so that the kernel's singular point u = 0 is a corner of every piece
+    that touches it; pieces away from 0 take a tensor Gauss rule, pieces with
+    the corner take three Duffy pyramids (u = t (L_e, L_f v, L_g w), Jacobian
+    t^2 L^3), which removes the 1/R^2 singularity of K and the 1/R of the
+    dynamic part of N.  The static part K_s of the N kernel (degree -3) is
+    integrated as K_s(u~) (W(t u~) - W(0)) / t; the remaining W(0) K_s / t is
+    the principal value over the cube around u = 0 (self offset; zero by
+    cubic symmetry) or vanishes (W(0) = 0 for the other offsets).  The self
+    offset then gets the point term (2/3) delta_pq Gram of
+    :func:`self_delta_term`.  Returns {m: (pwx, 6 | 3)}."""
+    wq, xq = gauss_1d(order)
+    t1, w1 = (xq + 1) / 2, wq / 2                       # Gauss on [0, 1]
+    T, V, Wv = np.meshgrid(t1, t1, t1, indexing="ij")
+    WT = (w1[:, None, None] * w1[None, :, None] * w1[None, None, :]).ravel()
+    T, V, Wv = T.ravel(), V.ravel(), Wv.ravel()
+    kfun = G_N if kernel == "N" else G_K
+    ncomp = 6 if kernel == "N" else 3
+    out = {}
+    for m in offsets:
+        m = tuple(int(v) for v in m)
+        acc = np.zeros((pwx, ncomp), dtype=complex)
+        pieces = [[(-res, 0.0), (0.0, res)] if m[d] == 0 else [(0.0, res), (res, 2 * res)] for d in range(3)]
+        for px in pieces[0]:
+            for py in pieces[1]:
+                for pz in pieces[2]:
+                    box = (px, py, pz)
+                    if all(0.0 in b for b in box):
+                        # corner at u = 0: signs and lengths of the box from that corner
+                        sg = np.array([1.0 if b[1] > 0 else -1.0 for b in box])
+                        L = np.array([b[1] - b[0] for b in box])
+                        for e in range(3):
+                            f, g = [d for d in range(3) if d != e]
+                            Ut = np.zeros((T.size, 3))                   # u~ = u / t
+                            Ut[:, e] = sg[e] * L[e]
+                            Ut[:, f] = sg[f] * L[f] * V
+                            Ut[:, g] = sg[g] * L[g] * Wv
+                            U = Ut * T[:, None]
+                            jac = L.prod() * T ** 2
+                            Wm = _moment_weights(U, m, res, pwx)
+                            Kf = kfun(U[:, 0], U[:, 1], U[:, 2], 0, 0, 0, k0)
+                            if kernel == "N":
+                                Ks = kfun(U[:, 0], U[:, 1], U[:, 2], 0, 0, 0, 0.0)
+                                Kst = kfun(Ut[:, 0], Ut[:, 1], Ut[:, 2], 0, 0, 0, 0.0)   # K_s(u~) = t^3 K_s(u)
+                                W0 = _moment_weights(np.zeros((1, 3)), m, res, pwx)
+                                acc += np.einsum("qc,ql->lc", (Kf - Ks) * (WT * jac)[:, None], Wm)
+                                acc += np.einsum("qc,ql->lc", Kst * (WT * L.prod())[:, None],
+                                                 (Wm - W0) / T[:, None])
+                            else:
+                                acc += np.einsum("qc,ql->lc", Kf * (WT * jac)[:, None], Wm)
+                    else:
+                        lo = np.array([b[0] for b in box])
+                        L = np.array([b[1] - b[0] for b in box])
+                        U = lo[None, :] + L[None, :] * np.stack([T, V, Wv], axis=1)
+                        Wm = _moment_weights(U, m, res, pwx)
+                        Kf = kfun(U[:, 0], U[:, 1], U[:, 2], 0, 0, 0, k0)
+                        acc += np.einsum("qc,ql->lc", Kf * (WT * L.prod())[:, None], Wm)
+        if kernel == "N" and m == (0, 0, 0):
+            acc += self_delta_term(res, pwx)
+        out[m] = acc
+    return out
+
+
 def assembly_op(n1, n2, n3, res, k0, pwl: bool, kernel: str = "N",
-                Np_far=4, Np_medium=8, self_term: str = "pointwise"):
+                Np_far=4, Np_medium=8, self_term: str = "pointwise", near: str = "standin"):
     """Restates src/src_integral_equations/src_vie/src_operators_vie/
     assembly_N.m:16-81 and assembly_K.m:16-81 (far, medium, near zones).
 
     Returns I_V with shape (n1, n2, n3, pwx, 6) for N, (..., 3) for K.
-    The near zone uses :func:`near_zone_standin`; self_term="distributional"
-    adds the point term of the N kernel at the self offset
-    (:func:`self_delta_term`; K has none).
+    near="standin": the near zone by :func:`near_zone_standin`, and
+    self_term="distributional" adds the point term of the N kernel at the
+    self offset (:func:`self_delta_term`; K has none); near="relative": the
+    near zone by :func:`near_zone_relative` (point term included).
     """
+    near_rule = near
     pwx = 10 if pwl else 1
     ncomp = 6 if kernel == "N" else 3
     I_V = np.zeros((n1, n2, n3, pwx, ncomp), dtype=complex)
@@ -227,13 +325,16 @@ def assembly_op(n1, n2, n3, res, k0, pwl: bool, kernel: str = "N",
                     continue
                 r_m = np.array([mx, my, mz], dtype=float) * res
                 I_V[mx, my, mz] = VV_op(W, X, Y, Z, Xp, Yp, Zp, k0, r_m, np.zeros(3), res, pwx, kernel)
-    nz = near_zone_standin(k0, res, pwx, kernel, near)
+    if self_term not in ("pointwise", "distributional") or near_rule not in ("standin", "relative"):
+        raise ValueError(f"bad self_term {self_term!r} or near {near_rule!r}")
+    if near_rule == "relative":
+        nz = near_zone_relative(k0, res, pwx, kernel, near)
+    else:
+        nz = near_zone_standin(k0, res, pwx, kernel, near)
     for m, v in nz.items():
         I_V[m] = v
-    if self_term == "distributional" and kernel == "N":
+    if near_rule == "standin" and self_term == "distributional" and kernel == "N":
         I_V[0, 0, 0] += self_delta_term(res, pwx)
-    elif self_term not in ("pointwise", "distributional"):
-        raise ValueError(f"self_term must be 'pointwise' or 'distributional', got {self_term!r}")
     return I_V
 
 

@@ -21,5 +21,8 @@ void shim_pad_grid(const double* src, const int* n, const int* m, long long nblk
 void shim_add_self_point_term(double* out, long long nD, int pwx, double res) {
   marie::green_host::add_self_point_term(out, nD, pwx, res);
 }
+void shim_near_zone_exact(double* iv, int n1, int n2, int n3, double res, double k0, int pwx, int isN, int order) {
+  marie::green_host::near_zone_exact(iv, n1, n2, n3, res, k0, pwx, isN != 0, order);
+}
 long long shim_remap(long long lin, const int* n, const int* m) { return marie::embed::remap_voxel(lin, n, m); }
 }

@@ -1,9 +1,11 @@
-"""The point term of the N kernel at the self offset on the GPU assembly
-(marie_assemble_green_ex with MARIE_GREEN_SELF_POINT_TERM, through the
-Python assemble_green(self_term="distributional")).
+"""The near-zone options of the GPU Green's-tensor assembly
+(marie_assemble_green_ex, through the Python assemble_green).
 
-* It adds exactly the oracle's self_delta_term to I_V(0,0,0) of N and
-  leaves every other entry, and K, as marie_assemble_green computes them.
+* MARIE_GREEN_SELF_POINT_TERM (self_term="distributional") adds exactly the
+  oracle's self_delta_term to I_V(0,0,0) of N and leaves every other entry,
+  and K, as marie_assemble_green computes them.
+* MARIE_GREEN_NEAR_EXACT (near="relative") gives the oracle's
+  near_zone_relative on the offsets {0,1}^3 (N and K) and leaves the rest.
 * Known answer: the GPU-assembled operator with it reproduces the internal
   field 3/(eps_r + 2) E0 of a quasi-static dielectric sphere (12^3 grid,
   1 cm voxels, r = 5 cm, 1 MHz) within the voxelisation error.
@@ -32,12 +34,28 @@ def test_self_point_term_flag(pwl):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pwl,kernel", [(False, "N"), (True, "N"), (True, "K")], ids=["pwc-N", "pwl-N", "pwl-K"])
+def test_near_exact_flag(pwl, kernel):
+    from marie_gb300 import assemble_green
+    n, res, freq = (5, 4, 3), 2e-3, 297.2e6
+    a = assemble_green(n, res, freq, pwl, kernel)
+    b = assemble_green(n, res, freq, pwl, kernel, near="relative")
+    near = [(x, y, z) for x in range(2) for y in range(2) for z in range(2)]
+    ref = O.near_zone_relative(O.em_constants(freq)["k0"], res, 10 if pwl else 1, kernel, near)
+    scale = np.abs(a).max()
+    for m in near:
+        assert np.abs(b[m] - ref[m]).max() <= 1e-12 * scale, m
+        b[m] = a[m]
+    assert np.allclose(b, a, rtol=0, atol=1e-13 * scale)
+
+
+@pytest.mark.gpu
 def test_quasi_static_sphere_field_gpu():
     from marie_gb300 import VieOperator, assemble_green, phantoms
     res, freq, er = 1e-2, 1e6, 50.0
     body = phantoms.sphere(12, res, 0.05, er, 0.0)
     emc = O.em_constants(freq)
-    iv = assemble_green(body.n, res, freq, False, "N", self_term="distributional")
+    iv = assemble_green(body.n, res, freq, False, "N", near="relative")
     Mr = body.Mr(freq)
     op = VieOperator(body.n, res, freq, body.idx_solution(False), Mr, iv, pwl=False, precisions=3, max_rhs=1)
     Ns = body.idxS.size
