@@ -38,6 +38,8 @@ def load():
             [ct.c_int] * 3 + [_D]
         lib.oracle_directfn_ea.argtypes = [_D] * 6 + [ct.c_int, ct.c_double, ct.c_double] + [_D] * 4 + \
             [ct.c_int] * 3 + [_D]
+        lib.oracle_directfn_va.argtypes = [_D] * 7 + [ct.c_int, ct.c_double, ct.c_double] + [_D] * 4 + \
+            [ct.c_int] * 3 + [_D]
         _lib = lib
     return _lib
 
@@ -97,3 +99,182 @@ def pwc_near_entries(k0, res, N=16):
     return {"self_xx": 4 * S_st - 4 * S_opp,
             "face_xx": 4 * S_ea - 4 * S_par,
             "face_yy": -S_st + 2 * S_opp - S_far2 + 2 * S_ea - 2 * S_par}
+
+
+# ---------------------------------------------------------------------------
+# The whole surface-surface near zone of assembly_N.m:56-81 (any near offset,
+# PWC and PWL): surface_surface_coeff_Nop.m + surface_surface_kernels_Nop.m
+# with coefficients_Nop.m and kernels_Nop.m, singular face pairs by DIRECTFN.
+# The face pairs are classified by their shared vertices (4: ST, 2: EA, 1:
+# VA, 0: regular) and the DIRECTFN point orders built from that, instead of
+# the hand tables of points_mapping.m.
+# ---------------------------------------------------------------------------
+
+_NX = [-1, 1, 0, 0, 0, 0]
+_NY = [0, 0, -1, 1, 0, 0]
+_NZ = [0, 0, 0, 0, -1, 1]
+_P = [1, 1, 1, 2, 2, 3]
+_Q = [1, 2, 3, 2, 3, 3]
+
+
+def _h(l, dx):
+    """Gradient of moment l (1-based: 1 const, 2 x/dx, 3 y/dx, 4 z/dx)."""
+    h = np.zeros(3)
+    if l > 1:
+        h[l - 2] = 1.0 / dx
+    return h
+
+
+def coefficients_Nop(dx, n, np_, p, q, l, lp, ker):
+    """coefficients_Nop.m:1-89."""
+    pp = np.eye(3)[p - 1]
+    qq = np.eye(3)[q - 1]
+    if ker == 1:
+        return float(np.dot(np.cross(n, pp), np.cross(np_, qq)))
+    if ker == 2:
+        return float(np.dot(np.cross(np.cross(_h(l, dx), pp), qq), n))
+    if ker == 3:
+        return float(np.dot(np.cross(pp, np.cross(_h(lp, dx), qq)), n))
+    a = np.cross(_h(l, dx), pp)
+    hp = _h(lp, dx)
+    return float(sum(np.dot(np.cross(a, np.eye(3)[j]), n) * np.dot(hp * qq[j], np_) for j in range(3)))
+
+
+def _face(c, f, dx):
+    """Normal and cyclic vertices of face f (0-based, surface_surface_kernels_Nop.m face order) of the voxel
+    centred at c."""
+    n = np.array([_NX[f], _NY[f], _NZ[f]], dtype=float)
+    a = int(np.argmax(np.abs(n)))
+    b, e = (a + 1) % 3, (a + 2) % 3
+    verts = []
+    for sb, se in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+        v = np.array(c, dtype=float)
+        v[a] += n[a] * dx / 2
+        v[b] += sb * dx / 2
+        v[e] += se * dx / 2
+        verts.append(v)
+    return n, verts
+
+
+def _rot(verts, first, second=None):
+    """Cyclic order of a square's vertices starting at `first` (then `second`
+    if given, else either neighbour)."""
+    k = next(i for i, v in enumerate(verts) if np.allclose(v, first))
+    fwd = [verts[(k + i) % 4] for i in range(4)]
+    bwd = [verts[(k - i) % 4] for i in range(4)]
+    if second is None or np.allclose(fwd[1], second):
+        return fwd
+    assert np.allclose(bwd[1], second)
+    return bwd
+
+
+def _kernel_regular(ker, Xo, Xs, k0, dx, rm, rn, l, lp, nsrc):
+    """kernels_Nop.m:1-122 at observation points Xo and source points Xs
+    (paired rows)."""
+    d = Xo - Xs
+    R = np.linalg.norm(d, axis=1)
+    G = np.exp(-1j * k0 * R) / (4 * np.pi * R)
+    G0 = 1 / (4 * np.pi * R)
+
+    def mom(l_, X, c):
+        return np.ones(len(X)) if l_ == 1 else (X[:, l_ - 2] - c[l_ - 2]) / dx
+    if ker == 1:
+        return mom(l, Xo, rm) * mom(lp, Xs, rn) * G
+    ff = d / (1j * k0) ** 2 * (-1j * k0 * G / R - G / R ** 2 + G0 / R ** 2)[:, None]
+    q2 = ff @ nsrc
+    if ker == 2:
+        return mom(lp, Xs, rn) * q2
+    if ker == 3:
+        return mom(l, Xo, rm) * q2
+    return (G - G0) / (1j * k0) ** 2
+
+
+def surface_near_zone(k0, dx, pwx, m, N=16, qg=16):
+    """I_V(m) (pwx, 6) of the N operator by the reference's surface-surface
+    formulation (surface_surface_kernels_Nop.m), singular integrals by the
+    reference's DIRECTFN; m in {0,1}^3 (observation voxel at m dx, source at
+    the origin)."""
+    L = 4 if pwx == 10 else 1
+    rm = np.array(m, dtype=float) * dx
+    rn = np.zeros(3)
+    w, x = O.gauss_1d(qg)
+    x, w = x / 2, w / 2
+    S, T = np.meshgrid(x, x, indexing="ij")
+    S, T, W2 = S.ravel(), T.ravel(), np.outer(w, w).ravel()
+    lib = load()
+    z3 = np.zeros(3)
+    Iss = np.zeros((L, L, 6), dtype=complex)
+    for f in range(6):
+        n, Vo = _face(rm, f, dx)
+        for fp in range(6):
+            np_, Vs = _face(rn, fp, dx)
+            shared = [v for v in Vs if any(np.allclose(v, u) for u in Vo)]
+            k = len(shared)
+            cache = {}
+
+            def integral(ker, l, lp):
+                key = (ker, l if ker in (1, 3) else 1, lp if ker in (1, 2) else 1)
+                if key in cache:
+                    return cache[key]
+                if k == 0:
+                    # regular: Gauss over both squares (vertex 0 + s e1 + t e2)
+                    def pts(V):
+                        e1, e2 = V[1] - V[0], V[3] - V[0]
+                        return V[0][None, :] + (S + 0.5)[:, None] * e1 + (T + 0.5)[:, None] * e2
+                    Po, Ps = pts(Vo), pts(Vs)
+                    Xo = np.repeat(Po, len(Ps), axis=0)
+                    Xs = np.tile(Ps, (len(Po), 1))
+                    Wq = np.repeat(W2, len(W2)) * np.tile(W2, len(W2)) * dx ** 4
+                    val = np.sum(Wq * _kernel_regular(ker, Xo, Xs, k0, dx, rm, rn, l, lp, np_))
+                else:
+                    out = np.zeros(2)
+                    lo, lpo = (l - 1 if ker in (1, 3) else 0), (lp - 1 if ker in (1, 2) else 0)
+                    if k == 4:
+                        r = _rot(Vs, Vs[0], Vs[1])
+                        cq = (r[0] + r[2]) / 2
+                        args = [r[0], r[1], r[2], r[3]]
+                        fn, cs, co = lib.oracle_directfn_st, cq, cq
+                    elif k == 2:
+                        e0, e1 = shared
+                        src = _rot(Vs, e0, e1)             # (r3, r4, r1, r2)
+                        obs = _rot(Vo, e1, e0)             # (r4, r3, r6, r5)
+                        r1, r2, r3, r4 = src[2], src[3], src[0], src[1]
+                        r6, r5 = obs[2], obs[3]
+                        args = [r1, r2, r3, r4, r5, r6]
+                        fn, cs, co = lib.oracle_directfn_ea, (r1 + r3) / 2, (r4 + r6) / 2
+                    else:
+                        v = shared[0]
+                        src = _rot(Vs, v)                  # (r3, r4, r1, r2)
+                        obs = _rot(Vo, v)                  # (r3, r5, r6, r7)
+                        r3, r4, r1, r2 = src
+                        r5, r6, r7 = obs[1], obs[2], obs[3]
+                        args = [r1, r2, r3, r4, r5, r6, r7]
+                        fn, cs, co = lib.oracle_directfn_va, (r1 + r3) / 2, (r3 + r6) / 2
+                    keep = [np.ascontiguousarray(a, dtype=float) for a in args + [cs, co, np_, n]]
+                    ptrs = [a.ctypes.data_as(_D) for a in keep]
+                    fn(*ptrs[:len(args)], N, k0, dx, *ptrs[len(args):], ker, lo, lpo, out.ctypes.data_as(_D))
+                    val = out[0] + 1j * out[1]
+                cache[key] = val
+                return val
+
+            for i in range(6):
+                for l in range(1, L + 1):
+                    for lp in range(1, L + 1):
+                        acc = 0.0
+                        c1 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], 0, 0, 1)
+                        if c1:
+                            acc += c1 * integral(1, l, lp)
+                        c2 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], l, 0, 2)
+                        if c2:
+                            acc += c2 * integral(2, 1, lp)
+                        c3 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], 0, lp, 3)
+                        if c3:
+                            acc += c3 * integral(3, l, 1)
+                        c4 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], l, lp, 4)
+                        if c4:
+                            acc += c4 * integral(4, 1, 1)
+                        Iss[l - 1, lp - 1, i] += acc
+    out = np.zeros((pwx, 6), dtype=complex)
+    for llp in range(pwx):
+        out[llp] = Iss[O.IND_L[llp], O.IND_LP[llp]]
+    return out

@@ -40,4 +40,16 @@ void oracle_directfn_ea(const double* r1, const double* r2, const double* r3, co
   out[1] = I[0].imag();
 }
 
+void oracle_directfn_va(const double* r1, const double* r2, const double* r3, const double* r4, const double* r5,
+                        const double* r6, const double* r7, int N, double k0, double dx, const double* c_src,
+                        const double* c_obs, const double* n_src, const double* n_obs, int ker, int l, int lp,
+                        double* out) {
+  double cq[3], cp[3], nq[3], np[3];
+  for (int i = 0; i < 3; ++i) { cq[i] = c_src[i]; cp[i] = c_obs[i]; nq[i] = n_src[i]; np[i] = n_obs[i]; }
+  std::complex<double> I[1];
+  create_VA(r1, r2, r3, r4, r5, r6, r7, N, N, N, N, k0, dx, cq, cp, nq, np, ker, l, lp, I);
+  out[0] = I[0].real();
+  out[1] = I[0].imag();
+}
+
 }  // extern "C"

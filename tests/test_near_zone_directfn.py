@@ -2,12 +2,15 @@
 
 oracle/Makefile compiles the reference's DIRECTFN C++ (the singular
 surface-surface integrals behind assembly_N.m:56-81) from the reference
-checkout into oracle/_ref; oracle/directfn_ref.py evaluates with it the
-surface-surface near zone of the PWC moment (self offset xx, face neighbour
-xx and yy).  The oracle's near_zone_relative (and hence the library's
-MARIE_GREEN_NEAR_EXACT cubature, equal to it to 1e-14 in
-test_green_host.py) must agree.  Skipped where the reference checkout or
-g++ is absent.
+checkout into oracle/_ref; oracle/directfn_ref.py restates the reference's
+surface-surface near zone (surface_surface_kernels_Nop.m with
+coefficients_Nop.m and kernels_Nop.m, singular face pairs through DIRECTFN
+ST / EA / VA) and a short face-pair form of its PWC entries.  The oracle's
+near_zone_relative (and hence the library's MARIE_GREEN_NEAR_EXACT cubature,
+equal to it to 1e-14 in test_green_host.py) must agree: every near offset
+of the PWC moment to 1e-12, the PWL moments (all ten pairs, six components)
+on the self, face and vertex offsets to the accuracy of DIRECTFN at order
+10.  Skipped where the reference checkout or g++ is absent.
 """
 import os
 import shutil
@@ -44,3 +47,22 @@ def test_pwc_near_zone_matches_directfn(directfn, freq, res):
     st = O.near_zone_standin(k0, res, 1, "N", [(0, 0, 0), (1, 0, 0)])
     assert abs(st[(0, 0, 0)][0, 0]) < 1e-3 * abs(ref["self_xx"])
     assert abs(st[(1, 0, 0)][0, 0] / ref["face_xx"] - 1) > 0.05
+
+
+NEAR = [(a, b, c) for a in range(2) for b in range(2) for c in range(2)]
+
+
+def test_surface_form_pwc_all_offsets(directfn):
+    k0 = O.em_constants(297.2e6)["k0"]
+    nz = O.near_zone_relative(k0, 2e-3, 1, "N", NEAR)
+    for m in NEAR:
+        ref = directfn.surface_near_zone(k0, 2e-3, 1, m, N=16, qg=12)
+        assert np.abs(nz[m] - ref).max() <= 1e-12 * np.abs(ref).max(), m
+
+
+@pytest.mark.parametrize("m,tol", [((0, 0, 0), 1e-10), ((1, 0, 0), 1e-8), ((1, 1, 1), 1e-8)])
+def test_surface_form_pwl(directfn, m, tol):
+    k0 = O.em_constants(297.2e6)["k0"]
+    ref = directfn.surface_near_zone(k0, 2e-3, 10, m, N=10, qg=8)
+    got = O.near_zone_relative(k0, 2e-3, 10, "N", [m])[m]
+    assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
