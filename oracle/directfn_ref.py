@@ -278,3 +278,129 @@ def surface_near_zone(k0, dx, pwx, m, N=16, qg=16):
     for llp in range(pwx):
         out[llp] = Iss[O.IND_L[llp], O.IND_LP[llp]]
     return out
+
+
+# --- the K operator: surface_surface_coeff_Kop.m / surface_surface_kernels_Kop.m
+_PK = [3, 1, 2]
+_QK = [2, 3, 1]
+
+
+def coefficients_Kop(dx, ko, n, np_, p, q, l, lp, ker):
+    """coefficients_Kop.m:1-89."""
+    pp = np.eye(3)[p - 1]
+    qq = np.eye(3)[q - 1]
+    if ker == 1:
+        return complex(np.dot(np.cross(pp, qq), np_))
+    if ker == 2:
+        return 1 / (1j * ko) ** 2 * np.dot(np_, np.dot(np.cross(qq, pp), _h(lp, dx)) * _h(l, dx))
+    if ker == 3:
+        return complex(np.dot(n, np_) * np.dot(_h(lp, dx), np.cross(pp, qq)))
+    h = _h(l, dx)
+    return complex(sum(np.dot(np.cross(qq, np.eye(3)[j]), np_) * np.dot(h * pp[j], n) for j in range(3)))
+
+
+def _kernel_regular_K(ker, Xo, Xs, k0, dx, rm, rn, l, lp, nobs):
+    """kernels_Kop.m:1-114 at paired observation / source points."""
+    d = Xo - Xs
+    R = np.linalg.norm(d, axis=1)
+    G = np.exp(-1j * k0 * R) / (4 * np.pi * R)
+    G0 = 1 / (4 * np.pi * R)
+
+    def mom(l_, X, c):
+        return np.ones(len(X)) if l_ == 1 else (X[:, l_ - 2] - c[l_ - 2]) / dx
+    ff = d / (1j * k0) ** 2 * (-1j * k0 * G / R - G / R ** 2 + G0 / R ** 2)[:, None]
+    if ker == 1:
+        return mom(l, Xo, rm) * mom(lp, Xs, rn) * (ff @ nobs)
+    if ker == 2:
+        return (ff - d / 2 * G0[:, None]) @ nobs
+    if ker == 3:
+        return mom(l, Xo, rm) * (G - G0) / (1j * k0) ** 2
+    return mom(lp, Xs, rn) * (G - G0) / (1j * k0) ** 2
+
+
+def surface_near_zone_K(k0, dx, pwx, m, N=16, qg=16):
+    """I_V(m) (pwx, 3) of the K operator by the reference's surface-surface
+    formulation (surface_surface_kernels_Kop.m: kernels 1-4 through DIRECTFN
+    kernel types 5-8 on singular face pairs), m in {0,1}^3."""
+    L = 4 if pwx == 10 else 1
+    rm = np.array(m, dtype=float) * dx
+    rn = np.zeros(3)
+    w, x = O.gauss_1d(qg)
+    x, w = x / 2, w / 2
+    S, T = np.meshgrid(x, x, indexing="ij")
+    S, T, W2 = S.ravel(), T.ravel(), np.outer(w, w).ravel()
+    lib = load()
+    Iss = np.zeros((L, L, 3), dtype=complex)
+    for f in range(6):
+        n, Vo = _face(rm, f, dx)
+        for fp in range(6):
+            np_, Vs = _face(rn, fp, dx)
+            shared = [v for v in Vs if any(np.allclose(v, u) for u in Vo)]
+            k = len(shared)
+            cache = {}
+
+            def integral(ker, l, lp):
+                if (ker, l, lp) in cache:
+                    return cache[(ker, l, lp)]
+                if k == 0:
+                    def pts(V):
+                        e1, e2 = V[1] - V[0], V[3] - V[0]
+                        return V[0][None, :] + (S + 0.5)[:, None] * e1 + (T + 0.5)[:, None] * e2
+                    Po, Ps = pts(Vo), pts(Vs)
+                    Xo = np.repeat(Po, len(Ps), axis=0)
+                    Xs = np.tile(Ps, (len(Po), 1))
+                    Wq = np.repeat(W2, len(W2)) * np.tile(W2, len(W2)) * dx ** 4
+                    val = np.sum(Wq * _kernel_regular_K(ker, Xo, Xs, k0, dx, rm, rn, l, lp, n))
+                else:
+                    out = np.zeros(2)
+                    dker = 4 + ker
+                    if k == 4:
+                        r = _rot(Vs, Vs[0], Vs[1])
+                        cq = (r[0] + r[2]) / 2
+                        args, fn, cs, co = [r[0], r[1], r[2], r[3]], lib.oracle_directfn_st, cq, cq
+                    elif k == 2:
+                        e0, e1 = shared
+                        src = _rot(Vs, e0, e1)
+                        obs = _rot(Vo, e1, e0)
+                        r1, r2, r3, r4 = src[2], src[3], src[0], src[1]
+                        r6, r5 = obs[2], obs[3]
+                        args, fn = [r1, r2, r3, r4, r5, r6], lib.oracle_directfn_ea
+                        cs, co = (r1 + r3) / 2, (r4 + r6) / 2
+                    else:
+                        v = shared[0]
+                        src = _rot(Vs, v)
+                        obs = _rot(Vo, v)
+                        r3, r4, r1, r2 = src
+                        r5, r6, r7 = obs[1], obs[2], obs[3]
+                        args, fn = [r1, r2, r3, r4, r5, r6, r7], lib.oracle_directfn_va
+                        cs, co = (r1 + r3) / 2, (r3 + r6) / 2
+                    keep = [np.ascontiguousarray(a, dtype=float) for a in args + [cs, co, np_, n]]
+                    ptrs = [a.ctypes.data_as(_D) for a in keep]
+                    fn(*ptrs[:len(args)], N, k0, dx, *ptrs[len(args):], dker, l - 1, lp - 1,
+                       out.ctypes.data_as(_D))
+                    val = out[0] + 1j * out[1]
+                cache[(ker, l, lp)] = val
+                return val
+
+            for i in range(3):
+                p, q = _PK[i], _QK[i]
+                for l in range(1, L + 1):
+                    for lp in range(1, L + 1):
+                        acc = 0.0
+                        c = coefficients_Kop(dx, k0, n, np_, p, q, 0, 0, 1)
+                        if c:
+                            acc += c * integral(1, l, lp)
+                        c = coefficients_Kop(dx, k0, n, np_, p, q, l, lp, 2)
+                        if c:
+                            acc += c * integral(2, 1, 1)
+                        c = coefficients_Kop(dx, k0, n, np_, p, q, 0, lp, 3)
+                        if c:
+                            acc += c * integral(3, l, 1)
+                        c = coefficients_Kop(dx, k0, n, np_, p, q, l, 0, 4)
+                        if c:
+                            acc += c * integral(4, 1, lp)
+                        Iss[l - 1, lp - 1, i] += acc
+    out = np.zeros((pwx, 3), dtype=complex)
+    for llp in range(pwx):
+        out[llp] = Iss[O.IND_L[llp], O.IND_LP[llp]]
+    return out

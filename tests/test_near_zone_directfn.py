@@ -66,3 +66,23 @@ def test_surface_form_pwl(directfn, m, tol):
     ref = directfn.surface_near_zone(k0, 2e-3, 10, m, N=10, qg=8)
     got = O.near_zone_relative(k0, 2e-3, 10, "N", [m])[m]
     assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
+
+
+def test_surface_form_K_pwc_all_offsets(directfn):
+    """The K operator (surface_surface_kernels_Kop.m, DIRECTFN kernel types
+    5-8): every near offset of the PWC moment (the self offset is zero on
+    both sides)."""
+    k0 = O.em_constants(297.2e6)["k0"]
+    nz = O.near_zone_relative(k0, 2e-3, 1, "K", NEAR)
+    ref = {m: directfn.surface_near_zone_K(k0, 2e-3, 1, m, N=12, qg=12) for m in NEAR}
+    scale = max(np.abs(v).max() for v in ref.values())
+    for m in NEAR:
+        assert np.abs(nz[m] - ref[m]).max() <= 1e-10 * scale, m
+
+
+@pytest.mark.parametrize("m", [(1, 0, 0), (1, 1, 1)])
+def test_surface_form_K_pwl(directfn, m):
+    k0 = O.em_constants(297.2e6)["k0"]
+    ref = directfn.surface_near_zone_K(k0, 2e-3, 10, m, N=10, qg=10)
+    got = O.near_zone_relative(k0, 2e-3, 10, "K", [m])[m]
+    assert np.abs(got - ref).max() <= 1e-7 * np.abs(ref).max()
