@@ -16,6 +16,10 @@
  *   [x, iter, resvec] = marie_mex('gmres', h, b, restart, tol, maxit, x0 [, mode])
  *                                                   % is_gmres_vie.m:1; b may be N_b x nrhs
  *   marie_mex('destroy', h)
+ *   I_V = marie_mex('assemble', [n1 n2 n3], PWX, res, freq, 'N' | 'K' [, 'exact' | 'standin'])
+ *       assembly_N.m / assembly_K.m on the GPU, (n1, n2, n3, pwx, 6 | 3) complex; near zone 'exact'
+ *       (default: the same integrals as the reference's DIRECTFN surface-surface near zone) or the
+ *       'standin' cubature
  * Inputs may be host double/single complex arrays or gpuArrays; outputs follow
  * the input ('like'), as in the reference.  Errors are raised with
  * mexErrMsgIdAndTxt('marie:<status>', ...), in the style of the reference's
@@ -212,11 +216,39 @@ static void cmd_gmres(int nlhs, mxArray** plhs, int nrhs, const mxArray** prhs, 
   }
 }
 
+/* I_V = marie_mex('assemble', [n1 n2 n3], PWX, res, freq, kernel [, near]) */
+static void cmd_assemble(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
+  (void)nlhs;
+  if (nrhs < 6) mexErrMsgIdAndTxt("marie:BAD_ARG", "assemble needs [n1 n2 n3], PWX, res, freq, 'N'|'K'");
+  if (!mxIsDouble(prhs[1]) || mxGetNumberOfElements(prhs[1]) != 3)
+    mexErrMsgIdAndTxt("marie:BAD_ARG", "grid size must be a 1x3 double");
+  const double* nd = mxGetDoubles(prhs[1]);
+  const int32_t n1 = (int32_t)nd[0], n2 = (int32_t)nd[1], n3 = (int32_t)nd[2];
+  const int pwl = scalar(prhs[2], "PWX") == 1.0;
+  const double res = scalar(prhs[3], "res"), freq = scalar(prhs[4], "freq");
+  char kern[8] = {0}, near[16] = {0};
+  if (!mxIsChar(prhs[5]) || mxGetString(prhs[5], kern, sizeof(kern)) || (strcmp(kern, "N") && strcmp(kern, "K")))
+    mexErrMsgIdAndTxt("marie:BAD_ARG", "kernel must be 'N' or 'K'");
+  int32_t flags = MARIE_GREEN_NEAR_EXACT;
+  if (nrhs > 6) {
+    if (!mxIsChar(prhs[6]) || mxGetString(prhs[6], near, sizeof(near)) ||
+        (strcmp(near, "exact") && strcmp(near, "standin")))
+      mexErrMsgIdAndTxt("marie:BAD_ARG", "near zone must be 'exact' or 'standin'");
+    if (!strcmp(near, "standin")) flags = 0;
+  }
+  if (n1 < 1 || n2 < 1 || n3 < 1) mexErrMsgIdAndTxt("marie:BAD_ARG", "grid edges must be positive");
+  const mwSize dims[5] = {(mwSize)n1, (mwSize)n2, (mwSize)n3, (mwSize)(pwl ? 10 : 1), (mwSize)(kern[0] == 'N' ? 6 : 3)};
+  plhs[0] = mxCreateNumericArray(5, dims, mxDOUBLE_CLASS, mxCOMPLEX);
+  check(marie_assemble_green_ex(n1, n2, n3, res, freq, pwl ? MARIE_PWL : MARIE_PWC, kern[0] == 'N' ? 0 : 1, flags,
+                                (double*)mxGetComplexDoubles(plhs[0])));
+}
+
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs < 1 || !mxIsChar(prhs[0])) mexErrMsgIdAndTxt("marie:BAD_ARG", "first argument must be a command string");
   char cmd[32];
   mxGetString(prhs[0], cmd, sizeof(cmd));
   if (!strcmp(cmd, "create")) { cmd_create(nlhs, plhs, nrhs, prhs); return; }
+  if (!strcmp(cmd, "assemble")) { cmd_assemble(nlhs, plhs, nrhs, prhs); return; }
   if (nrhs < 2) mexErrMsgIdAndTxt("marie:BAD_ARG", "missing handle");
   marie_vie* h = get_handle(prhs[1]);
   if (!strcmp(cmd, "destroy")) { check(marie_vie_destroy(h)); return; }
