@@ -436,7 +436,7 @@ def run_uneven(args):
     for d in uneven_instances():
         n, res, freq, nl = d["n"], d["res"], d["freq"], d["nloops"]
         body = phantoms.ellipsoid_phantom(n, res, seed=100 + d["i"], scale=d["scale"])
-        iv = assemble_green(body.n, res, freq, False, "N")
+        iv = assemble_green(body.n, res, freq, False, "N", near=args.near)
         op = VieOperator(body.n, res, freq, body.idx_solution(False), body.Mr(freq), iv, pwl=False,
                          precisions=2 | 4, max_rhs=nl)
         del iv
@@ -496,7 +496,7 @@ def run_uneven(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32 accumulation) + FP64 refinement",
         "data": "synthetic (seeded phantoms, GPU-assembled Green's tensors, loop incident fields)",
         "config": {"workload": "16 PWC ellipsoid phantoms, edges from {48..128} at 2 mm, 128/297.2 MHz, 1-8 loops",
-                   "loops_total": total, "restart": 50, "tol": 1e-6,
+                   "loops_total": total, "restart": 50, "tol": 1e-6, "near_zone": args.near,
                    "schedule": "bodies one after another on one stream, each one batched solve of its loops"},
         "e2e": {"value": round(total / (ms_e2e * 1e-3), 4), "unit": "solves/s",
                 "h2d_bytes_per_step": int(sum(b.numel() * 16 for _, b in hb)),
