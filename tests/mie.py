@@ -14,10 +14,14 @@ def mie_internal(points, a, k, m, nmax=None):
     relative refractive index m, free-space wavenumber k, for the incident
     E = x exp(i k z); nmax terms (Wiscombe's rule by default)."""
     x = k * a
-    if nmax is None: nmax = int(x + 4 * x ** (1/3) + 10)
+    if nmax is None:
+        nmax = int(x + 4 * x ** (1 / 3) + 10)
     mx = m * x
-    r = np.linalg.norm(points, axis=1); th = np.arccos(np.clip(points[:, 2] / r, -1, 1)); ph = np.arctan2(points[:, 1], points[:, 0])
-    mu = np.cos(th); rho = m * k * r
+    r = np.linalg.norm(points, axis=1)
+    th = np.arccos(np.clip(points[:, 2] / r, -1, 1))
+    ph = np.arctan2(points[:, 1], points[:, 0])
+    mu = np.cos(th)
+    rho = m * k * r
     E = np.zeros((len(r), 3), complex)
     pi_prev, pi_cur = np.zeros_like(mu), np.ones_like(mu)
     for n in range(1, nmax + 1):
@@ -25,17 +29,17 @@ def mie_internal(points, a, k, m, nmax=None):
             pi_new = ((2*n-1)/(n-1)) * mu * pi_cur - (n/(n-1)) * pi_prev
             pi_prev, pi_cur = pi_cur, pi_new
         tau = n * mu * pi_cur - (n + 1) * pi_prev
-        jn = spherical_jn(n, x); jnp = spherical_jn(n, x, derivative=True)
-        yn = spherical_yn(n, x); ynp = spherical_yn(n, x, derivative=True)
-        hn = jn + 1j*yn; hnp = jnp + 1j*ynp
+        jn, jnp = spherical_jn(n, x), spherical_jn(n, x, derivative=True)
+        yn, ynp = spherical_yn(n, x), spherical_yn(n, x, derivative=True)
+        hn, hnp = jn + 1j * yn, jnp + 1j * ynp
         xh_p = hn + x*hnp            # [x h_n(x)]'
         xj_p = jn + x*jnp
-        jm = spherical_jn(n, mx); jmp = spherical_jn(n, mx, derivative=True)
+        jm, jmp = spherical_jn(n, mx), spherical_jn(n, mx, derivative=True)
         mxj_p = jm + mx*jmp          # [mx j_n(mx)]'
         cn = (jn*xh_p - hn*xj_p) / (jm*xh_p - hn*mxj_p)
         dn = (m*jn*xh_p - m*hn*xj_p) / (m**2*jm*xh_p - hn*mxj_p)
         En = 1j**n * (2*n+1) / (n*(n+1))
-        z = spherical_jn(n, rho); zp = spherical_jn(n, rho, derivative=True)
+        z, zp = spherical_jn(n, rho), spherical_jn(n, rho, derivative=True)
         rz_p = z + rho*zp            # [rho z_n]'
         # M_o1n and N_e1n (spherical components r, theta, phi)
         M = np.stack([np.zeros_like(z), np.cos(ph)*pi_cur*z, -np.sin(ph)*tau*z], axis=1)
