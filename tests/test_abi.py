@@ -122,3 +122,32 @@ def test_header_compiles_as_c(tmp_path):
     r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-c", str(src),
                         "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_embedded_grid_descriptors_are_validated_on_the_callers_grid(lib):
+    """A grid with a prime edge above 31 goes through the embedding branch of
+    marie_vie_create; its descriptor is checked on the caller's grid first."""
+    n1 = 37
+    nD = n1 * 4 * 4
+    mr = np.ones(2 * nD)
+    dense = np.zeros(2 * nD * 6)
+    idxS = np.array([0, 1, nD], dtype=np.int64)               # nD is outside the 37x4x4 grid
+    idx = np.concatenate([idxS + c * nD for c in range(3)])
+    d = _desc(n1=n1, n_b=9, idx_solution=idx.ctypes.data_as(ct.POINTER(ct.c_int64)),
+              Mr=mr.ctypes.data_as(_lib.c_double_p), dense_N=dense.ctypes.data_as(_lib.c_double_p))
+    st, h = _create(lib, d)
+    assert st == 1 and "outside" in _lib.last_error() and not h.value
+    idxS = np.array([0, 1, 2], dtype=np.int64)
+    idx = np.concatenate([idxS + c * nD for c in range(3)])
+    d = _desc(n1=n1, n_b=9, idx_solution=idx.ctypes.data_as(ct.POINTER(ct.c_int64)), precisions=5,
+              Mr=mr.ctypes.data_as(_lib.c_double_p), dense_N=dense.ctypes.data_as(_lib.c_double_p))
+    st, h = _create(lib, d)
+    assert st == 1 and "exclusive" in _lib.last_error()
+
+
+def test_assemble_green_ex_rejects_unknown_flags(lib):
+    out = np.zeros(2 * 8 * 6)
+    st = lib.marie_assemble_green_ex(2, 2, 2, 2e-3, 297.2e6, 0, 0, 4, out.ctypes.data_as(_lib.c_double_p))
+    assert st == 1 and "flags" in _lib.last_error()
+    st = lib.marie_assemble_green_ex(0, 2, 2, 2e-3, 297.2e6, 0, 0, 2, out.ctypes.data_as(_lib.c_double_p))
+    assert st == 1
