@@ -10,10 +10,13 @@ numpy/scipy port using every host core:
   the circulant Green spectra, C inverse FFTs + crop, contrast epilogue)
   + one classical Gram-Schmidt Arnoldi step (is_iter_gmres_vie.m:15-19).
 
-The Green blocks are pre-expanded (the reference re-expands its Tucker
-factors inside every product, which is slower), and their values are seeded
-synthetic arrays: the timing of FFTs and elementwise products does not depend
-on the values.  Sizes, layouts and operation counts are the workload's.
+Two variants: "pre-expanded" Green blocks (the fastest CPU form of the
+algorithm), and "reference" (tucker_ranks given), which re-expands a Tucker
+block inside every block product as mvp_N_pwl_tucker.m:31 does (three mode
+products, nmp.m:1-21, of an r1 x r2 x r3 core with r x 2n factors).  Values
+are seeded synthetic arrays: the timing of FFTs, GEMMs and elementwise
+products does not depend on them.  Sizes, layouts and operation counts are
+the workload's.
 """
 from __future__ import annotations
 
@@ -32,8 +35,19 @@ def _chunks(n, k):
     return [(i, min(n, i + step)) for i in range(0, n, step)]
 
 
+def _expand(G, U1, U2, U3):
+    """Tucker block G x1 U1^T x2 U2^T x3 U3^T on the (2n)^3 grid (nmp.m:1-21
+    applied three times, as mvp_N_pwl_tucker.m:31)."""
+    A = np.tensordot(G, U1, axes=([0], [0]))       # r2 r3 m
+    A = np.tensordot(A, U2, axes=([0], [0]))       # r3 m m
+    return np.tensordot(A, U3, axes=([0], [0]))    # m m m
+
+
 def time_iteration(n: int, pwl: bool, steps: int = 1, warmup: int = 0, budget_s: float = 30.0,
-                   body_fraction: float = 0.117, k_arnoldi: int = 25, restart: int = 50, seed: int = 0):
+                   body_fraction: float = 0.117, k_arnoldi: int = 25, restart: int = 50, seed: int = 0,
+                   tucker_ranks=None):
+    """tucker_ranks: None (pre-expanded blocks) or (r1, r2, r3) of the Tucker
+    blocks that every block product re-expands (the reference's form)."""
     cores = os.cpu_count() or 1
     rng = np.random.default_rng(seed)
     C = 12 if pwl else 3
@@ -52,6 +66,12 @@ def time_iteration(n: int, pwl: bool, steps: int = 1, warmup: int = 0, budget_s:
     V = rng.standard_normal((Nb, k_arnoldi + 1)) + 1j * rng.standard_normal((Nb, k_arnoldi + 1))
     pool = ThreadPoolExecutor(max_workers=cores)
     parts = _chunks(M, cores)
+    tk = None
+    if tucker_ranks is not None:
+        r1, r2, r3 = (int(v) for v in tucker_ranks)
+        tk = [((rng.standard_normal((r1, r2, r3)) + 1j * rng.standard_normal((r1, r2, r3))),
+               *(rng.standard_normal((r, m)) + 1j * rng.standard_normal((r, m)) for r in (r1, r2, r3)))
+              for _ in range(nspec)]
 
     def matvec(xb):
         Jp = np.zeros(n ** 3 * C, complex)
@@ -62,8 +82,13 @@ def time_iteration(n: int, pwl: bool, steps: int = 1, warmup: int = 0, budget_s:
         out = np.empty_like(Jp)
         acc = np.empty(M, complex)
         for p in range(C):
-            terms = [(tab[p][q][0], spec[tab[p][q][1][1] % nspec].reshape(-1), fJ[q])
-                     for q in range(C) if tab[p][q] is not None]
+            if tk is None:
+                terms = [(tab[p][q][0], spec[tab[p][q][1][1] % nspec].reshape(-1), fJ[q])
+                         for q in range(C) if tab[p][q] is not None]
+            else:
+                # the reference re-expands the block of every product (mvp_N_pwl_tucker.m:31)
+                terms = [(tab[p][q][0], _expand(*tk[tab[p][q][1][1] % nspec]).reshape(-1), fJ[q])
+                         for q in range(C) if tab[p][q] is not None]
 
             def work(lohi):
                 lo, hi = lohi
@@ -103,4 +128,4 @@ def time_iteration(n: int, pwl: bool, steps: int = 1, warmup: int = 0, budget_s:
             break
     pool.shutdown()
     return {"sec_per_iter": float(np.mean(times)), "iters_timed": len(times), "cores": cores, "k": k_arnoldi,
-            "Nb": Nb}
+            "Nb": Nb, "variant": "reference (Tucker re-expanded per product)" if tk is not None else "pre-expanded"}
