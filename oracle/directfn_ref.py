@@ -189,90 +189,96 @@ def _kernel_regular(ker, Xo, Xs, k0, dx, rm, rn, l, lp, nsrc):
     return (G - G0) / (1j * k0) ** 2
 
 
-def surface_near_zone(k0, dx, pwx, m, N=16, qg=16):
-    """I_V(m) (pwx, 6) of the N operator by the reference's surface-surface
-    formulation (surface_surface_kernels_Nop.m), singular integrals by the
-    reference's DIRECTFN; m in {0,1}^3 (observation voxel at m dx, source at
-    the origin)."""
-    L = 4 if pwx == 10 else 1
-    rm = np.array(m, dtype=float) * dx
-    rn = np.zeros(3)
+def _pair_integral(Vo, Vs, n, np_, dker, l0, lp0, regular_fn, k0, dx, N, quad):
+    """One face-pair integral of the surface form: by the reference's DIRECTFN
+    (kernel type dker, 0-based moments l0, lp0) if the two squares share a
+    vertex, an edge or everything, else by a tensor Gauss rule of the
+    kernel regular_fn(Xo, Xs) (paired observation / source points)."""
+    shared = [v for v in Vs if any(np.allclose(v, u) for u in Vo)]
+    k = len(shared)
+    if k == 0:
+        S, T, W2 = quad
+
+        def pts(V):
+            e1, e2 = V[1] - V[0], V[3] - V[0]
+            return V[0][None, :] + (S + 0.5)[:, None] * e1 + (T + 0.5)[:, None] * e2
+        Po, Ps = pts(Vo), pts(Vs)
+        Xo = np.repeat(Po, len(Ps), axis=0)
+        Xs = np.tile(Ps, (len(Po), 1))
+        Wq = np.repeat(W2, len(W2)) * np.tile(W2, len(W2)) * dx ** 4
+        return np.sum(Wq * regular_fn(Xo, Xs))
+    lib = load()
+    if k == 4:                                       # ST: one square
+        r = _rot(Vs, Vs[0], Vs[1])
+        cq = (r[0] + r[2]) / 2
+        args, fn, cs, co = [r[0], r[1], r[2], r[3]], lib.oracle_directfn_st, cq, cq
+    elif k == 2:                                     # EA: source (r3, r4, r1, r2), observation (r4, r3, r6, r5)
+        e0, e1 = shared
+        src = _rot(Vs, e0, e1)
+        obs = _rot(Vo, e1, e0)
+        r1, r2, r3, r4 = src[2], src[3], src[0], src[1]
+        r6, r5 = obs[2], obs[3]
+        args, fn = [r1, r2, r3, r4, r5, r6], lib.oracle_directfn_ea
+        cs, co = (r1 + r3) / 2, (r4 + r6) / 2        # singular_EA_lin.m
+    else:                                            # VA: source (r3, r4, r1, r2), observation (r3, r5, r6, r7)
+        src = _rot(Vs, shared[0])
+        obs = _rot(Vo, shared[0])
+        r3, r4, r1, r2 = src
+        r5, r6, r7 = obs[1], obs[2], obs[3]
+        args, fn = [r1, r2, r3, r4, r5, r6, r7], lib.oracle_directfn_va
+        cs, co = (r1 + r3) / 2, (r3 + r6) / 2        # singular_VA_lin.m
+    keep = [np.ascontiguousarray(a, dtype=float) for a in args + [cs, co, np_, n]]
+    ptrs = [a.ctypes.data_as(_D) for a in keep]
+    out = np.zeros(2)
+    fn(*ptrs[:len(args)], N, k0, dx, *ptrs[len(args):], dker, l0, lp0, out.ctypes.data_as(_D))
+    return out[0] + 1j * out[1]
+
+
+def _gauss_squares(qg):
     w, x = O.gauss_1d(qg)
     x, w = x / 2, w / 2
     S, T = np.meshgrid(x, x, indexing="ij")
-    S, T, W2 = S.ravel(), T.ravel(), np.outer(w, w).ravel()
-    lib = load()
-    z3 = np.zeros(3)
+    return S.ravel(), T.ravel(), np.outer(w, w).ravel()
+
+
+def surface_near_zone(k0, dx, pwx, m, N=16, qg=16):
+    """I_V(m) (pwx, 6) of the N operator by the reference's surface-surface
+    formulation (surface_surface_kernels_Nop.m: kernels 1-4, DIRECTFN kernel
+    types 1-4 on the singular face pairs); m in {0,1}^3 (observation voxel at
+    m dx, source at the origin)."""
+    L = 4 if pwx == 10 else 1
+    rm, rn = np.array(m, dtype=float) * dx, np.zeros(3)
+    quad = _gauss_squares(qg)
     Iss = np.zeros((L, L, 6), dtype=complex)
     for f in range(6):
         n, Vo = _face(rm, f, dx)
         for fp in range(6):
             np_, Vs = _face(rn, fp, dx)
-            shared = [v for v in Vs if any(np.allclose(v, u) for u in Vo)]
-            k = len(shared)
             cache = {}
 
             def integral(ker, l, lp):
-                key = (ker, l if ker in (1, 3) else 1, lp if ker in (1, 2) else 1)
-                if key in cache:
-                    return cache[key]
-                if k == 0:
-                    # regular: Gauss over both squares (vertex 0 + s e1 + t e2)
-                    def pts(V):
-                        e1, e2 = V[1] - V[0], V[3] - V[0]
-                        return V[0][None, :] + (S + 0.5)[:, None] * e1 + (T + 0.5)[:, None] * e2
-                    Po, Ps = pts(Vo), pts(Vs)
-                    Xo = np.repeat(Po, len(Ps), axis=0)
-                    Xs = np.tile(Ps, (len(Po), 1))
-                    Wq = np.repeat(W2, len(W2)) * np.tile(W2, len(W2)) * dx ** 4
-                    val = np.sum(Wq * _kernel_regular(ker, Xo, Xs, k0, dx, rm, rn, l, lp, np_))
-                else:
-                    out = np.zeros(2)
-                    lo, lpo = (l - 1 if ker in (1, 3) else 0), (lp - 1 if ker in (1, 2) else 0)
-                    if k == 4:
-                        r = _rot(Vs, Vs[0], Vs[1])
-                        cq = (r[0] + r[2]) / 2
-                        args = [r[0], r[1], r[2], r[3]]
-                        fn, cs, co = lib.oracle_directfn_st, cq, cq
-                    elif k == 2:
-                        e0, e1 = shared
-                        src = _rot(Vs, e0, e1)             # (r3, r4, r1, r2)
-                        obs = _rot(Vo, e1, e0)             # (r4, r3, r6, r5)
-                        r1, r2, r3, r4 = src[2], src[3], src[0], src[1]
-                        r6, r5 = obs[2], obs[3]
-                        args = [r1, r2, r3, r4, r5, r6]
-                        fn, cs, co = lib.oracle_directfn_ea, (r1 + r3) / 2, (r4 + r6) / 2
-                    else:
-                        v = shared[0]
-                        src = _rot(Vs, v)                  # (r3, r4, r1, r2)
-                        obs = _rot(Vo, v)                  # (r3, r5, r6, r7)
-                        r3, r4, r1, r2 = src
-                        r5, r6, r7 = obs[1], obs[2], obs[3]
-                        args = [r1, r2, r3, r4, r5, r6, r7]
-                        fn, cs, co = lib.oracle_directfn_va, (r1 + r3) / 2, (r3 + r6) / 2
-                    keep = [np.ascontiguousarray(a, dtype=float) for a in args + [cs, co, np_, n]]
-                    ptrs = [a.ctypes.data_as(_D) for a in keep]
-                    fn(*ptrs[:len(args)], N, k0, dx, *ptrs[len(args):], ker, lo, lpo, out.ctypes.data_as(_D))
-                    val = out[0] + 1j * out[1]
-                cache[key] = val
-                return val
+                if (ker, l, lp) not in cache:
+                    reg = (lambda Xo, Xs: _kernel_regular(ker, Xo, Xs, k0, dx, rm, rn, l, lp, np_))
+                    cache[(ker, l, lp)] = _pair_integral(Vo, Vs, n, np_, ker, l - 1, lp - 1, reg, k0, dx, N, quad)
+                return cache[(ker, l, lp)]
 
             for i in range(6):
+                p, q = _P[i], _Q[i]
                 for l in range(1, L + 1):
                     for lp in range(1, L + 1):
                         acc = 0.0
-                        c1 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], 0, 0, 1)
-                        if c1:
-                            acc += c1 * integral(1, l, lp)
-                        c2 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], l, 0, 2)
-                        if c2:
-                            acc += c2 * integral(2, 1, lp)
-                        c3 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], 0, lp, 3)
-                        if c3:
-                            acc += c3 * integral(3, l, 1)
-                        c4 = coefficients_Nop(dx, n, np_, _P[i], _Q[i], l, lp, 4)
-                        if c4:
-                            acc += c4 * integral(4, 1, 1)
+                        c = coefficients_Nop(dx, n, np_, p, q, 0, 0, 1)
+                        if c:
+                            acc += c * integral(1, l, lp)
+                        c = coefficients_Nop(dx, n, np_, p, q, l, 0, 2)
+                        if c:
+                            acc += c * integral(2, 1, lp)
+                        c = coefficients_Nop(dx, n, np_, p, q, 0, lp, 3)
+                        if c:
+                            acc += c * integral(3, l, 1)
+                        c = coefficients_Nop(dx, n, np_, p, q, l, lp, 4)
+                        if c:
+                            acc += c * integral(4, 1, 1)
                         Iss[l - 1, lp - 1, i] += acc
     out = np.zeros((pwx, 6), dtype=complex)
     for llp in range(pwx):
@@ -323,64 +329,21 @@ def surface_near_zone_K(k0, dx, pwx, m, N=16, qg=16):
     formulation (surface_surface_kernels_Kop.m: kernels 1-4 through DIRECTFN
     kernel types 5-8 on singular face pairs), m in {0,1}^3."""
     L = 4 if pwx == 10 else 1
-    rm = np.array(m, dtype=float) * dx
-    rn = np.zeros(3)
-    w, x = O.gauss_1d(qg)
-    x, w = x / 2, w / 2
-    S, T = np.meshgrid(x, x, indexing="ij")
-    S, T, W2 = S.ravel(), T.ravel(), np.outer(w, w).ravel()
-    lib = load()
+    rm, rn = np.array(m, dtype=float) * dx, np.zeros(3)
+    quad = _gauss_squares(qg)
     Iss = np.zeros((L, L, 3), dtype=complex)
     for f in range(6):
         n, Vo = _face(rm, f, dx)
         for fp in range(6):
             np_, Vs = _face(rn, fp, dx)
-            shared = [v for v in Vs if any(np.allclose(v, u) for u in Vo)]
-            k = len(shared)
             cache = {}
 
             def integral(ker, l, lp):
-                if (ker, l, lp) in cache:
-                    return cache[(ker, l, lp)]
-                if k == 0:
-                    def pts(V):
-                        e1, e2 = V[1] - V[0], V[3] - V[0]
-                        return V[0][None, :] + (S + 0.5)[:, None] * e1 + (T + 0.5)[:, None] * e2
-                    Po, Ps = pts(Vo), pts(Vs)
-                    Xo = np.repeat(Po, len(Ps), axis=0)
-                    Xs = np.tile(Ps, (len(Po), 1))
-                    Wq = np.repeat(W2, len(W2)) * np.tile(W2, len(W2)) * dx ** 4
-                    val = np.sum(Wq * _kernel_regular_K(ker, Xo, Xs, k0, dx, rm, rn, l, lp, n))
-                else:
-                    out = np.zeros(2)
-                    dker = 4 + ker
-                    if k == 4:
-                        r = _rot(Vs, Vs[0], Vs[1])
-                        cq = (r[0] + r[2]) / 2
-                        args, fn, cs, co = [r[0], r[1], r[2], r[3]], lib.oracle_directfn_st, cq, cq
-                    elif k == 2:
-                        e0, e1 = shared
-                        src = _rot(Vs, e0, e1)
-                        obs = _rot(Vo, e1, e0)
-                        r1, r2, r3, r4 = src[2], src[3], src[0], src[1]
-                        r6, r5 = obs[2], obs[3]
-                        args, fn = [r1, r2, r3, r4, r5, r6], lib.oracle_directfn_ea
-                        cs, co = (r1 + r3) / 2, (r4 + r6) / 2
-                    else:
-                        v = shared[0]
-                        src = _rot(Vs, v)
-                        obs = _rot(Vo, v)
-                        r3, r4, r1, r2 = src
-                        r5, r6, r7 = obs[1], obs[2], obs[3]
-                        args, fn = [r1, r2, r3, r4, r5, r6, r7], lib.oracle_directfn_va
-                        cs, co = (r1 + r3) / 2, (r3 + r6) / 2
-                    keep = [np.ascontiguousarray(a, dtype=float) for a in args + [cs, co, np_, n]]
-                    ptrs = [a.ctypes.data_as(_D) for a in keep]
-                    fn(*ptrs[:len(args)], N, k0, dx, *ptrs[len(args):], dker, l - 1, lp - 1,
-                       out.ctypes.data_as(_D))
-                    val = out[0] + 1j * out[1]
-                cache[(ker, l, lp)] = val
-                return val
+                if (ker, l, lp) not in cache:
+                    reg = (lambda Xo, Xs: _kernel_regular_K(ker, Xo, Xs, k0, dx, rm, rn, l, lp, n))
+                    cache[(ker, l, lp)] = _pair_integral(Vo, Vs, n, np_, 4 + ker, l - 1, lp - 1, reg, k0, dx, N,
+                                                         quad)
+                return cache[(ker, l, lp)]
 
             for i in range(3):
                 p, q = _PK[i], _QK[i]
