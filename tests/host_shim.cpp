@@ -24,5 +24,10 @@ void shim_add_self_point_term(double* out, long long nD, int pwx, double res) {
 void shim_near_zone_exact(double* iv, int n1, int n2, int n3, double res, double k0, int pwx, int isN, int order) {
   marie::green_host::near_zone_exact(iv, n1, n2, n3, res, k0, pwx, isN != 0, order);
 }
+void shim_gauss01(int n, double* x, double* w) {
+  std::vector<double> xv, wv;
+  marie::green_host::gauss01(n, xv, wv);
+  for (int i = 0; i < n; ++i) { x[i] = xv[i]; w[i] = wv[i]; }
+}
 long long shim_remap(long long lin, const int* n, const int* m) { return marie::embed::remap_voxel(lin, n, m); }
 }

@@ -41,7 +41,20 @@ def shim(tmp_path_factory):
     lib.shim_add_self_point_term.argtypes = [D, ct.c_longlong, ct.c_int, ct.c_double]
     lib.shim_near_zone_exact.argtypes = [D, ct.c_int, ct.c_int, ct.c_int, ct.c_double, ct.c_double, ct.c_int,
                                          ct.c_int, ct.c_int]
+    lib.shim_gauss01.argtypes = [ct.c_int, D, D]
     return lib
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 16, 24])
+def test_host_gauss_rule(shim, n):
+    """The host Gauss-Legendre rule on [0, 1] of the near-zone cubature equals
+    numpy's and integrates polynomials of degree 2n-1 exactly."""
+    x, w = np.zeros(n), np.zeros(n)
+    shim.shim_gauss01(n, x.ctypes.data_as(D), w.ctypes.data_as(D))
+    xr, wr = np.polynomial.legendre.leggauss(n)
+    assert np.allclose(x, (xr + 1) / 2, atol=1e-15) and np.allclose(w, wr / 2, atol=1e-15)
+    for deg in range(2 * n):
+        assert abs(np.sum(w * x ** deg) - 1.0 / (deg + 1)) < 1e-14
 
 
 @pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
