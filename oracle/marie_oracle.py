@@ -5,14 +5,24 @@ C-ABI, or the Python host package) imports, links or executes this module.
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` use it, and only as the checker / the timed CPU reference.
 
-Parity status: *parity unpinned*.  The reference hot path is MATLAB
-(``.m`` files calling ``fftn``/``svd``/``mldivide``); MATLAB and Octave are
-not available, and the reference ships no tests, golden vectors or fixtures
-for this path.  This restatement follows the reference line by line (each
-function cites the file:line it restates, paths relative to the reference
-project root) and is pinned instead by algebraic identities (adjoint and
-transpose identities, Tucker exactness, an independent direct-sum
-convolution) in ``tests/test_oracle.py``.
+Parity status of the hot path: *parity unpinned*.  The reference hot path
+is MATLAB (``.m`` files calling ``fftn``/``svd``/``mldivide``); MATLAB and
+Octave are not available, and the reference ships no tests, golden vectors
+or fixtures for this path.  This restatement follows the reference line by
+line (each function cites the file:line it restates, paths relative to the
+reference project root) and is pinned instead by algebraic identities
+(adjoint and transpose identities, Tucker exactness, an independent
+direct-sum convolution) in ``tests/test_oracle.py``, and by known answers
+(quasi-static sphere, Mie series) in ``tests/test_green_host.py`` and
+``tests/test_physics_sphere.py``.
+
+Operator generation: far and medium zones restate assembly_N.m /
+assembly_K.m; the near zone is either the staggered stand-in
+(:func:`near_zone_standin`, what the GPU assembly computes by default) or
+:func:`near_zone_relative`, an independent cubature of the same integrals
+that is pinned to the reference's own surface-surface near zone with its
+DIRECTFN C++ compiled from source (``oracle/directfn_ref.py``,
+``tests/test_near_zone_directfn.py``).
 
 Conventions are MATLAB's: arrays are indexed (x, y, z, component) and
 flattened column-major (``order='F'``); index vectors are 0-based here where
