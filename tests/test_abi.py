@@ -151,3 +151,23 @@ def test_assemble_green_ex_rejects_unknown_flags(lib):
     assert st == 1 and "flags" in _lib.last_error()
     st = lib.marie_assemble_green_ex(0, 2, 2, 2e-3, 297.2e6, 0, 0, 2, out.ctypes.data_as(_lib.c_double_p))
     assert st == 1
+
+
+def test_embedded_descriptor_reaches_the_device_step(lib):
+    """A valid descriptor on a grid with a prime edge (37) runs the host-side
+    embedding (padding of Mr, idx_solution and the operator; the Tucker
+    factors re-derived for the 48 x 16 x 16 grid) and the embedded grid's
+    own validation, and stops only where a GPU is needed."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("needs a machine without a GPU")
+    from helpers import Problem
+    from marie_gb300 import VieOperator
+    P = Problem((37, 10, 9), False, seed=3)
+    for dense in (False, True):
+        N = P.IV_N if dense else P.TN
+        K = P.IV_K if dense else P.TK
+        with pytest.raises(_lib.MarieError) as e:
+            VieOperator(P.n, P.res, P.freq, P.dims["idx_solution"], P.Mr, N, K, pwl=False, precisions=2 | 4,
+                        max_rhs=1)
+        assert e.value.status == 6 and "CUDA device" in str(e.value)
