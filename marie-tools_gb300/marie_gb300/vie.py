@@ -92,6 +92,22 @@ def mvp_invG_pwl(T, res):
     return T / _gram(True, res).reshape((1,) * (T.ndim - 1) + (-1,))
 
 
+def assembly_N(n1, n2, n3, res, freq, PWX: int, near: str = "relative"):
+    """I_V = assembly_N(MREDM, n1, n2, n3) (assembly_N.m:1-83) on the GPU:
+    (n1, n2, n3, pwx, 6) complex, far and medium zones by the reference's
+    Gauss rules, near zone by the accurate cubature that matches its DIRECTFN
+    surface-surface terms ("standin": the staggered stand-in)."""
+    from .operator import assemble_green
+    return assemble_green((n1, n2, n3), res, freq, PWX == 1, "N", near=near)
+
+
+def assembly_K(n1, n2, n3, res, freq, PWX: int, near: str = "relative"):
+    """I_V = assembly_K(MREDM, n1, n2, n3) (assembly_K.m) on the GPU:
+    (n1, n2, n3, pwx, 3) complex, as :func:`assembly_N`."""
+    from .operator import assemble_green
+    return assemble_green((n1, n2, n3), res, freq, PWX == 1, "K", near=near)
+
+
 def parse_inputs(PWX: int) -> dict:
     """The VIE entries of the function-handle table of parse_inputs.m:6-37."""
     pwl = PWX == 1
