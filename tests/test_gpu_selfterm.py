@@ -67,3 +67,18 @@ def test_quasi_static_sphere_field_gpu():
     Ex = (x.cpu().numpy()[:Ns] / (emc["ce"] * Mcb)).real
     assert abs(Ex.mean() / (3.0 / (er + 2.0)) - 1.0) < 0.15, Ex.mean()
     op.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pwl,kernel", [(False, "N"), (True, "N"), (False, "K"), (True, "K")],
+                         ids=["pwc-N", "pwl-N", "pwc-K", "pwl-K"])
+def test_gpu_assembly_matches_oracle(pwl, kernel):
+    """marie_assemble_green (far and medium zones by the Gauss rules of
+    assembly_N.m / assembly_K.m, near zone by the stand-in) against the
+    oracle's restatement on the same grid, FP64 both sides."""
+    from marie_gb300 import assemble_green
+    n, res, freq = (5, 4, 3), 2e-3, 297.2e6
+    got = assemble_green(n, res, freq, pwl, kernel)
+    ref = O.assembly_op(*n, res, O.em_constants(freq)["k0"], pwl, kernel)
+    assert got.shape == ref.shape
+    assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
