@@ -11,6 +11,10 @@
 namespace marie {
 namespace green_host {
 
+// (l, l') of the ten moment products (VV_Nop.m:27-28), 0 = the constant
+constexpr int kL10[10] = {0, 1, 2, 3, 0, 0, 0, 1, 1, 2};
+constexpr int kLp10[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+
 // The point term of the N kernel at the self offset: its six components are
 // those of curl curl (g I), and as distributions d_p d_q g = PV(...) -
 // (1/3) delta_pq delta(r), lap g = -k0^2 g - delta(r), so curl curl (g I) =
@@ -19,17 +23,11 @@ namespace green_host {
 // res^3/12, res^3/12, res^3/12), the diagonal of mvp_G_pwl.m:5) to the xx, yy,
 // zz components (k = 0, 3, 5) of I_V(0,0,0).  The surface-surface near zone
 // of assembly_N.m:56-81 contains this term; the cubature of k_vv does not.
-// (l, l') of the ten moment products (VV_Nop.m:27-28), 0 = the constant
-constexpr int kL10[10] = {0, 1, 2, 3, 0, 0, 0, 1, 1, 2};
-constexpr int kLp10[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
-
 inline void add_self_point_term(double* out_host, int64_t nD, int pwx, double res) {
-  const int* kL = kL10;
-  const int* kLp = kLp10;
   const double r3 = res * res * res;
   for (int llp = 0; llp < pwx; ++llp) {
-    if (kL[llp] != kLp[llp]) continue;
-    const double g = (2.0 / 3.0) * (kL[llp] == 0 ? r3 : r3 / 12.0);
+    if (kL10[llp] != kLp10[llp]) continue;
+    const double g = (2.0 / 3.0) * (kL10[llp] == 0 ? r3 : r3 / 12.0);
     for (int k : {0, 3, 5}) out_host[2 * ((int64_t)(llp + pwx * k) * nD)] += g;   // (0,0,0) of block (llp, k)
   }
 }
