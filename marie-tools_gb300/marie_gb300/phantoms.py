@@ -1,9 +1,10 @@
-"""Seeded synthetic bodies, materials and coil placements (host-side set-up).
+"""Bodies, materials, input files and coil placements (host-side set-up).
 
-The reference reads bodies from RHBM .mat files (geo_body_domain.m:5-13);
-these generators produce the same data (voxel grid, idxS, epsilon_r, sigma)
-for the benchmark shapes: a homogeneous sphere and an ellipsoid phantom with
-random inner ellipsoids, plus loop-coil placements.
+The reference reads bodies from RHBM .mat files (geo_body_domain.m:5-13) named
+in JSON input files (load_inputs.m); load_rhbm and load_inputs read those
+formats.  The seeded generators produce the same data (voxel grid, idxS,
+epsilon_r, sigma) for the benchmark shapes: a homogeneous sphere and an
+ellipsoid phantom with random inner ellipsoids, plus loop-coil placements.
 """
 from __future__ import annotations
 
@@ -59,6 +60,40 @@ def _finish(n, res, origin, er, se, mask):
     er = np.where(mask, er, 1.0)
     se = np.where(mask, se, 0.0)
     return Body(tuple(int(v) for v in n), res, origin, er, se, idxS)
+
+
+# Gyromagnetic ratio / (2 pi) [Hz/T] of the nuclei MARIE simulates
+# (em_constants.m:3-60; physical constants, kept as the reference tabulates them)
+GAMMA0 = {"1H": 42.577478518e6, "2H": 6.536e6, "3HE": 32.434e6, "13C": 10.705e6, "15N": -4.316e6,
+          "17O": -5.772e6, "23NA": 11.262e6, "25MG": -2.614e6, "31P": 17.235e6, "35CL": 4.171e6,
+          "39K": 1.250e6, "59CO": 10.054e6, "79BR": 10.666e6, "87RB": 13.932e6, "129XE": 11.777e6}
+
+
+def larmor_frequency(B0: float, nucleus: str = "1H") -> float:
+    """emc.freq = |gamma0| * B0 (em_constants.m:70)."""
+    key = nucleus.upper()
+    if key not in GAMMA0:
+        raise ValueError(f"unknown nucleus {nucleus!r}")
+    return abs(GAMMA0[key]) * float(B0)
+
+
+def load_inputs(path, bodies_root=None) -> dict:
+    """The VIE-relevant fields of a MARIE input file (JSON, load_inputs.m:6-
+    60): B0, nucleus and the Larmor frequency, the basis (PWX 1 = PWL), the
+    body file (resolved against bodies_root, default <inputs dir>/../bodies),
+    and the solver / quadrature settings load_inputs.m fixes (GMRES tol 1e-5,
+    HOSVD tol 1e-7, 4 / 8 / 15 points for the far / medium / near zones)."""
+    import json
+    from pathlib import Path
+    path = Path(path)
+    d = json.loads(path.read_text())
+    root = Path(bodies_root) if bodies_root is not None else path.resolve().parent.parent / "bodies"
+    pwx = int(d["Basis_Functions_VIE"])
+    out = dict(B0=float(d["B0"]), nucleus=d["Nucleus"], freq=larmor_frequency(d["B0"], d["Nucleus"]),
+               PWX=pwx, pwl=pwx == 1, body_file=root / d["BodyFile"] if d.get("BodyFile") else None,
+               coil_file=d.get("CoilFile", ""), wire_file=d.get("WireFile", ""), shield_file=d.get("ShieldFile", ""),
+               tol=1e-5, tol_HOSVD=1e-7, Np_1D_far_V=4, Np_1D_medium_V=8, Np_1D_near_S=15)
+    return out
 
 
 def load_rhbm(path) -> Body:

@@ -75,3 +75,25 @@ def test_reference_bodies(name, n, ns):
     smooth = [_smooth31(v) for v in n]
     # 73 is prime: the cylinder's grid runs embedded (80 x 80 x 96); 121 = 11^2 runs as given
     assert smooth == ([True] * 3 if name == "Multilayer_Sphere" else [False, False, True])
+
+
+def test_load_inputs_synthetic(tmp_path):
+    import json
+    (tmp_path / "inputs").mkdir()
+    f = tmp_path / "inputs" / "inp.json"
+    f.write_text(json.dumps({"B0": 7.0, "Nucleus": "1H", "Basis_Functions_VIE": 0, "BodyFile": "x/b.mat",
+                             "CoilFile": "", "WireFile": "w.msh", "ShieldFile": "", "TMD": 1, "BasisFile": ""}))
+    inp = phantoms.load_inputs(f)
+    assert abs(inp["freq"] - 42.577478518e6 * 7.0) < 1e-3 and inp["pwl"] is False
+    assert inp["body_file"].resolve() == (tmp_path / "bodies" / "x" / "b.mat").resolve()
+    assert phantoms.larmor_frequency(3.0, "31p") == 17.235e6 * 3.0
+
+
+@pytest.mark.skipif(not (REF / "data" / "inputs").is_dir(), reason="reference input files not present")
+def test_reference_input_file():
+    """The reference's own input file: 1H at 3.0063 T is 128 MHz (the first
+    configuration's frequency), PWL basis, and its body file loads."""
+    inp = phantoms.load_inputs(REF / "data" / "inputs" / "inp_MSphere_HeadCoil1z.json")
+    assert abs(inp["freq"] - 128.0e6) < 0.1e6 and inp["pwl"] is True
+    b = phantoms.load_rhbm(inp["body_file"])
+    assert b.n == (121, 121, 121)
