@@ -1,0 +1,50 @@
+"""The loop right-hand side against the reference's own wire-coupling kernels
+(Assemble_tri_coupling_matrix_N_{x,y,z}.cpp, compiled from the reference
+checkout by oracle/Makefile; oracle/wire_ref.py).
+
+The library's loop kernel (k_loops, checked against the oracle's
+loop_field / incident_moments in the GPU tests) models a uniform unit
+current.  The reference's kernels with unit coefficients carry a sawtooth
+current of mean 1: its field component along the wire direction agrees with
+the uniform one to 0.1% 1-4 cm from the wire, while the sawtooth's line and
+point charges add radial and axial components that the uniform current does
+not have (up to 2.4x the tangential one at 1 cm).  Skipped where the
+reference checkout or g++ is absent.
+"""
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import marie_oracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+REF = Path(os.environ.get("MARIE_REFERENCE_ROOT", "/root/reference"))
+
+
+@pytest.fixture(scope="module")
+def wire():
+    if not (REF / "src").is_dir() or not shutil.which("g++") or not shutil.which("make"):
+        pytest.skip("reference checkout or toolchain not present")
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), f"REF={REF}"], check=True)
+    from oracle import wire_ref
+    return wire_ref
+
+
+def test_loop_field_along_the_wire_matches_reference(wire):
+    freq, res, radius, nseg = 297.2e6, 2e-3, 0.05, 64
+    emc = O.em_constants(freq)
+    centre, normal = np.zeros(3), np.array([0.0, 0.0, 1.0])
+    pts = np.array([[x, 0.0, -d] for d in (0.01, 0.02, 0.04) for x in (0.03, 0.05, 0.07)])
+    ref = wire.loop_field_reference(pts, centre, normal, radius, nseg, res, emc["k0"])
+    mid, dl = O.loop_points(centre, normal, radius, nseg)
+    ours = O.incident_moments(pts, res, False,
+                              lambda q: O.loop_field(q, mid, dl, emc["k0"], emc["omega"], emc["mu0"])).reshape(3, -1).T
+    # in the plane y = 0 the wire direction is y: the uniform current's field is y only
+    assert np.all(np.abs(ours[:, [0, 2]]) < 1e-9 * np.abs(ours[:, 1]).max())
+    assert np.all(np.abs(ref[:, 1] / ours[:, 1] - 1) < 2e-3)
+    # the sawtooth's charges: radial / axial components of the reference's field
+    assert np.abs(ref[:, [0, 2]]).max() > 0.5 * np.abs(ref[:, 1]).max()
