@@ -1,5 +1,5 @@
 """The loop right-hand side against the reference's own wire-coupling kernels
-(Assemble_tri_coupling_matrix_N_{x,y,z}.cpp, compiled from the reference
+(Assemble_tri_coupling_matrix_N_{x,y,z,y1,y2,y3}.cpp, compiled from the reference
 checkout by oracle/Makefile; oracle/wire_ref.py).
 
 The library's loop kernel (k_loops, checked against the oracle's
@@ -48,3 +48,24 @@ def test_loop_field_along_the_wire_matches_reference(wire):
     assert np.all(np.abs(ref[:, 1] / ours[:, 1] - 1) < 2e-3)
     # the sawtooth's charges: radial / axial components of the reference's field
     assert np.abs(ref[:, [0, 2]]).max() > 0.5 * np.abs(ref[:, 1]).max()
+
+
+def test_loop_field_pwl_moments_match_reference(wire):
+    """PWL moments of the wire-direction component (N_y, N_y1, N_y2, N_y3:
+    the constant and the x-, y-, z-linear moments): the constant and the x-
+    and z-moments agree to 2e-3 of the constant one; the y-moment, zero for
+    the uniform current by symmetry, is the sawtooth's charge field."""
+    freq, res, radius, nseg = 297.2e6, 2e-3, 0.05, 64
+    emc = O.em_constants(freq)
+    centre, normal = np.zeros(3), np.array([0.0, 0.0, 1.0])
+    pts = np.array([[x, 0.0, -d] for d in (0.01, 0.02) for x in (0.03, 0.05, 0.07)])
+    rp, rn, r2 = wire.loop_bases(centre, normal, radius, nseg)
+    ref = np.stack([wire.tri_coupling(v, pts, rp, rn, r2, res, emc["k0"]).sum(axis=1)
+                    for v in ("y", "y1", "y2", "y3")], axis=1)
+    ref[:, 1:] *= 12                      # voxel average of E f_l -> coefficient (int f_l^2 = 1/12)
+    mid, dl = O.loop_points(centre, normal, radius, nseg)
+    ours = O.incident_moments(pts, res, True, lambda q: O.loop_field(q, mid, dl, emc["k0"], emc["omega"],
+                                                                     emc["mu0"])).reshape(3, 4, -1)[1].T
+    scale = np.abs(ours[:, 0])[:, None]
+    assert np.all(np.abs(ours[:, [0, 1, 3]] - ref[:, [0, 1, 3]]) <= 2e-3 * scale)
+    assert np.all(np.abs(ours[:, 2]) < 1e-9 * scale[:, 0]) and np.abs(ref[:, 2]).max() > 1e-3 * scale.max()
