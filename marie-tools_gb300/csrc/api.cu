@@ -219,7 +219,7 @@ static int env_int(const char* name, int dflt) {
 }
 
 template <typename T>
-static void choose_tiles(marie_vie* h, PrecState<T>& ps) {
+static marie_status choose_tiles(marie_vie* h, PrecState<T>& ps) {
   const int n3 = h->n3, C = h->C;
   const int sz = (int)sizeof(cplx<T>);
   int W = 16;
@@ -227,13 +227,35 @@ static void choose_tiles(marie_vie* h, PrecState<T>& ps) {
   // MARIE_Z_TILE: z-pass tile width (power of two <= 16) if its shared
   // memory fits one CTA (227 KB)
   const int wz = env_int("MARIE_Z_TILE", 0);
-  const size_t lim = 227 * 1024;
+  const size_t lim = kSmemOptin;
   if (wz >= 1 && wz <= 16 && (wz & (wz - 1)) == 0 && (size_t)n3 * (2 * C * wz + 2) * sz <= lim &&
       kz4_smem<T>(n3, C, wz) <= lim)
     W = wz;
+  // The generic passes (any grid; K and K^H on every grid) with the
+  // narrowest row tiles and a bundle of W right-hand sides must fit one CTA's
+  // shared memory; narrow W until they do, and refuse the grid at create
+  // when even W = 1 does not (a pass would otherwise fail to launch midway
+  // through a matvec).  The float-float state runs the four-step passes only.
+  if constexpr (!std::is_same<T, ff>::value) {
+    auto need = [&](int w) { return generic_smem(h->n1, h->n2, n3, C, sz, 1, 1, 1, w); };
+    while (W > 1) {
+      const GenericSmem g = need(W);
+      if (g.x <= lim && g.y <= lim && g.z <= lim) break;
+      W /= 2;
+    }
+    const GenericSmem g = need(W);
+    if (g.x > lim || g.y > lim || g.z > lim) {
+      set_error("grid %d x %d x %d (%s, %s) needs %zu / %zu / %zu bytes of shared memory in the x / y / z "
+                "passes, more than the %zu a CTA can hold; use smaller edges (complex128 PWL: n3 <= %d)",
+                h->n1, h->n2, n3, C == 12 ? "PWL" : "PWC", sz == 16 ? "complex128" : "complex64", g.x, g.y,
+                g.z, lim, (int)(lim / ((size_t)(2 * C + 2) * 16)));
+      return MARIE_ERR_BAD_ARG;
+    }
+  }
   ps.TX = W;      // Wz
   ps.TY = 0;
   ps.TXY = 0;
+  return MARIE_OK;
 }
 
 struct CallTiles {
@@ -257,6 +279,12 @@ static CallTiles call_tiles(const marie_vie* h, const PrecState<T>& ps, int nr, 
   t.TY = std::max(1, std::min(h->n2, wxy / t.R));
   t.TXY = std::max(1, std::min(2 * h->n1, wxy / t.R));
   t.TX = std::max(1, std::min(2 * h->n1, Wz / t.R));
+  if (!fast) {   // generic passes: keep every tile within one CTA's shared memory
+    const size_t sz = sizeof(cplx<T>);
+    t.TY = std::min(t.TY, generic_tile_cap(h->n1, 1, t.R, sz));
+    t.TXY = std::min(t.TXY, generic_tile_cap(h->n2, 1, t.R, sz));
+    t.TX = std::min(t.TX, generic_tile_cap(h->n3, h->C, t.R, sz));
+  }
   return t;
 }
 
@@ -623,7 +651,7 @@ static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
       for (int64_t s = 0; s < h->Ns; ++s) chiff[s] = cplx<ff>{prec_from<ff>(chi[s].x), prec_from<ff>(chi[s].y)};
       if ((st = dev_alloc(h, (void**)&ps.chi, h->Ns * sizeof(cplx<ff>))) != MARIE_OK) return fail(st);
       cudaMemcpy(ps.chi, chiff.data(), h->Ns * sizeof(cplx<ff>), cudaMemcpyHostToDevice);
-      choose_tiles(h, ps);
+      if ((st = choose_tiles(h, ps)) != MARIE_OK) return fail(st);
       if ((st = alloc_workspace(h, ps)) != MARIE_OK) return fail(st);
     } else if (pr == 0) {
       PrecState<double>& ps = h->p64;
@@ -632,7 +660,7 @@ static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
       if ((st = build_axis(h, h->n3, ps.az)) != MARIE_OK) return fail(st);
       if ((st = dev_alloc(h, (void**)&ps.chi, h->Ns * sizeof(cplx<double>))) != MARIE_OK) return fail(st);
       cudaMemcpy(ps.chi, chi.data(), h->Ns * sizeof(cplx<double>), cudaMemcpyHostToDevice);
-      choose_tiles(h, ps);
+      if ((st = choose_tiles(h, ps)) != MARIE_OK) return fail(st);
       if ((st = alloc_workspace(h, ps)) != MARIE_OK) return fail(st);
     } else {
       PrecState<float>& ps = h->p32;
@@ -643,7 +671,7 @@ static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
       for (int64_t s = 0; s < h->Ns; ++s) chif[s] = cplx<float>{(float)chi[s].x, (float)chi[s].y};
       if ((st = dev_alloc(h, (void**)&ps.chi, h->Ns * sizeof(cplx<float>))) != MARIE_OK) return fail(st);
       cudaMemcpy(ps.chi, chif.data(), h->Ns * sizeof(cplx<float>), cudaMemcpyHostToDevice);
-      choose_tiles(h, ps);
+      if ((st = choose_tiles(h, ps)) != MARIE_OK) return fail(st);
       if ((st = alloc_workspace(h, ps)) != MARIE_OK) return fail(st);
     }
   }

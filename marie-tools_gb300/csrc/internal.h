@@ -136,6 +136,9 @@ marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaS
 
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
 
+// Largest dynamic shared memory a CTA may opt into on sm_100-family GPUs.
+constexpr size_t kSmemOptin = 227 * 1024;
+
 // Opt a kernel into the large dynamic shared-memory carve-out once per
 // device (the attribute is per device; a process may drive several).
 // `done` is the kernel's own flag word: bit d set once device d is done.
@@ -145,8 +148,26 @@ inline void smem_opt_in_device(const void* fn, std::atomic<uint64_t>& done) {
   cudaGetDevice(&dev);
   const uint64_t bit = 1ull << (dev & (kMaxDevices - 1));
   if (done.load(std::memory_order_acquire) & bit) return;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOptin);
   done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
+// Dynamic shared memory of the generic x, y and z passes (matvec.cuh) with
+// row tiles TY / TXY / TX and bundle size R: each holds its axis' twiddles
+// plus 2*tile*R (times C for z) padded sequences of length n.
+struct GenericSmem {
+  size_t x, y, z;
+};
+inline GenericSmem generic_smem(int n1, int n2, int n3, int C, size_t sz, int TY, int TXY, int TX, int R) {
+  return {(size_t)(n1 + (size_t)n1 * (2 * (size_t)TY * R + 1)) * sz,
+          (size_t)(n2 + (size_t)n2 * (2 * (size_t)TXY * R + 1)) * sz,
+          (size_t)(n3 + (size_t)n3 * (2 * (size_t)C * TX * R + 1)) * sz};
+}
+// Largest row tile t (>= 1) with n * (2 * mult * t * R + 2) elements of sz
+// bytes within kSmemOptin; 1 when even t = 1 does not fit (the caller checks).
+inline int generic_tile_cap(int n, int mult, int R, size_t sz) {
+  const long v = ((long)(kSmemOptin / sz / (size_t)n) - 2) / (2L * mult * R);
+  return (int)(v < 1 ? 1 : (v > (1 << 20) ? (1 << 20) : v));
 }
 
 // Every grid edge is 16*NB with NB <= 8: the four-step passes apply.

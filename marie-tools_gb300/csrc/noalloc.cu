@@ -101,7 +101,14 @@ marie_status na_setup(int dev, NaPtrs** out) {
     const void* fns[] = {(const void*)k_fwd_x<float>, (const void*)k_fwd_y<float>,
                          (const void*)k_inv_y<float>, (const void*)k_inv_x<float>,
                          (const void*)k_z<float, true, 0>, (const void*)k_z<float, false, 0>};
-    for (const void* f : fns) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    for (const void* f : fns) {
+      e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemOptin);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("noalloc: cudaFuncSetAttribute (shared-memory opt-in) failed: %s", cudaGetErrorString(e));
+        return MARIE_ERR_CUDA;
+      }
+    }
     P.ready = true;
   }
   *out = &P;
@@ -137,6 +144,22 @@ extern "C" marie_status marie_vie_apply_N_noalloc(int32_t n1, int32_t n2, int32_
     set_error("noalloc: grid edge with a prime factor above 31 (unsupported FFT length)");
     return MARIE_ERR_NOT_SUPPORTED;
   }
+  // tiles: the same rule as the handle path for one complex64 right-hand
+  // side, narrowed where a pass would not fit one CTA's shared memory; a
+  // grid that does not fit even with one-row tiles is refused before any
+  // launch
+  const size_t sz = sizeof(cplx<float>);
+  int W = 16;
+  while (W > 1 && (size_t)n3 * (2 * C * W + 1) * sz > 100 * 1024) W /= 2;
+  const int TY = std::min(std::max(1, std::min(n2, 16)), generic_tile_cap(n1, 1, 1, sz));
+  const int TXY = std::min(std::max(1, std::min(2 * n1, 16)), generic_tile_cap(n2, 1, 1, sz));
+  const int TX = std::min(std::max(1, std::min(2 * n1, W)), generic_tile_cap(n3, C, 1, sz));
+  const GenericSmem sm = generic_smem(n1, n2, n3, C, sz, TY, TXY, TX, 1);
+  if (sm.x > kSmemOptin || sm.y > kSmemOptin || sm.z > kSmemOptin) {
+    set_error("noalloc: grid %dx%dx%d (%s) needs %zu / %zu / %zu bytes of shared memory in the x / y / z passes, "
+              "more than the %zu a CTA can hold", n1, n2, n3, pwl ? "PWL" : "PWC", sm.x, sm.y, sm.z, kSmemOptin);
+    return MARIE_ERR_BAD_ARG;
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
@@ -171,16 +194,10 @@ extern "C" marie_status marie_vie_apply_N_noalloc(int32_t n1, int32_t n2, int32_
   a.T1 = (cplx<float>*)P->scratch;
   a.S = a.T1 + per;
   a.G = (const cplx<float>*)green_octant;
-  // tiles: the same rule as the handle path for one complex64 right-hand side
-  int W = 16;
-  while (W > 1 && (size_t)n3 * (2 * C * W + 1) * sizeof(cplx<float>) > 100 * 1024) W /= 2;
-  a.TY = std::max(1, std::min(n2, 16));
-  a.TXY = std::max(1, std::min(2 * n1, 16));
-  a.TX = std::max(1, std::min(2 * n1, W));
-  const size_t sz = sizeof(cplx<float>);
-  const size_t smx = (size_t)(n1 + (size_t)n1 * (2 * a.TY + 1)) * sz;
-  const size_t smy = (size_t)(n2 + (size_t)n2 * (2 * a.TXY + 1)) * sz;
-  const size_t smz = (size_t)(n3 + (size_t)n3 * (2 * C * a.TX + 1)) * sz;
+  a.TY = TY;
+  a.TXY = TXY;
+  a.TX = TX;
+  const size_t smx = sm.x, smy = sm.y, smz = sm.z;
   dim3 gx((n2 + a.TY - 1) / a.TY, n3, C);
   dim3 gy((2 * n1 + a.TXY - 1) / a.TXY, n3, C);
   dim3 gz((2 * n1 + a.TX - 1) / a.TX, 2 * n2, 1);
