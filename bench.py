@@ -36,13 +36,13 @@ sys.path[:0] = [str(ROOT), str(ROOT / "marie-tools_gb300")]
 
 WORKLOADS = {
     "ellipsoid128": dict(n=128, res=2e-3, freq=297.2e6, pwl=True, nrhs=64, tol=1e-6, phantom="ellipsoid",
-                 fp64_iters=13.0, tucker_ranks=(13, 13, 13),
+                 fp64_iters=183.1, tucker_ranks=(13, 13, 13),
                  desc="ellipsoid phantom 128^3 @ 2 mm, PWL, 297.2 MHz, 64 loop-port RHS"),
     "ellipsoid96": dict(n=96, res=2e-3, freq=297.2e6, pwl=True, nrhs=1, tol=1e-6, phantom="ellipsoid",
-                 fp64_iters=13.0, tucker_ranks=(13, 13, 13),
+                 fp64_iters=172.0, tucker_ranks=(13, 13, 13),
                  desc="ellipsoid phantom 96^3 @ 2 mm, PWL, 297.2 MHz, 1 loop RHS"),
     "sphere32": dict(n=32, res=5e-3, freq=128e6, pwl=False, nrhs=1, tol=1e-6, phantom="sphere",
-                 fp64_iters=9.0, desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
+                 fp64_iters=66.0, desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
 }
 METRIC = "GMRES solves/s at 128^3 PWL, 1e-6 resid (mixed c64/FP64-refined, 64-RHS batch)"
 
@@ -63,9 +63,15 @@ def metric_of(wl):
 # on 24^3 (12.0) and 48^3 (13.2) grids, rounded down (larger grids have
 # larger ranks, so the reference arm is not made slower than it is).
 # fp64_iters (per workload above): FP64 GMRES(50) iterations per right-hand
-# side to 1e-6, measured by this library's complex128 solver (the algorithm
-# of is_gmres_vie.m; the 'iters' of our arm's 'fp64_gpu' field); they turn
-# the reference arm's per-iteration time into solves/s.
+# side to 1e-6 on the workload's own operator (Green's tensor with the
+# accurate near zone), measured by this library's complex128 solver, which
+# follows is_gmres_vie.m / is_iter_gmres_vie.m step for step and matches
+# the oracle's iteration counts on every case the tests compare: 128^3, the
+# mean over the first 16 loop ports (171-190); 96^3, the one loop; 32^3, the
+# plane wave (two restart cycles).  Our arm re-measures them in every run
+# ('fp64_gpu.iters_mean'); the reference arm, which runs the CPU port of the
+# reference's algorithm and cannot afford a full 128^3 FP64 solve on the
+# host, turns its per-iteration time into solves/s with them.
 
 
 def _dist():
@@ -139,7 +145,7 @@ def build_problem(wl, rank, torch):
         body = phantoms.ellipsoid_phantom(n, res, seed=0)
     emc = phantoms.em_constants(freq)
     t0 = time.time()
-    ivN = assemble_green(body.n, res, freq, pwl, "N", near=wl.get("near", "standin"))
+    ivN = assemble_green(body.n, res, freq, pwl, "N", near=wl.get("near", "relative"))
     t_asm = time.time() - t0
     # complex64 inner solves + complex128 (float-float arithmetic) residuals
     op = VieOperator(body.n, res, freq, body.idx_solution(pwl), body.Mr(freq), ivN, pwl=pwl,
@@ -192,9 +198,7 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
     green = U * (n + 1) ** 3 * s            # octant spectrum, read once per launch
     alg = units * per_rhs + green
     achieved = alg / (ms_z * 1e-3) / 1e9
-    # ncu dram bytes (read + write) of one 16-RHS z-pass launch of this
-    # workload (profiles/k4_zp_c64_128pwl_16rhs_dram.md)
-    traffic = ZTRAFFIC_128PWL_16RHS if (wl["pwl"] and n == 128 and units == 16) else None
+    traffic = None
     four_step = n % 16 == 0 and 16 <= n <= 128
     name = (f"k4_zp<{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
     # FP32 work of the same launch: per right-hand side and (kx, ky) column,
@@ -211,9 +215,6 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
             "traffic": traffic, "alg_bytes_per_launch": int(alg), "launch_ms": round(ms_z, 4),
             "units_per_launch": units, "peak_source": peak_kind,
             "fp32": {"flops_per_launch": int(flops), "achieved_tflops": round(flops / (ms_z * 1e-3) / 1e12, 2)}}
-
-
-ZTRAFFIC_128PWL_16RHS = 26.14e9
 
 
 def run_ours(args, wl):
@@ -263,11 +264,13 @@ def run_ours(args, wl):
     # chunked solve)
     b_host = b.cpu().pin_memory()
     x_host = torch.empty_like(b_host).pin_memory()
-    op.gmres_host(b_host, out=x_host, **kw)      # warm-up of the host path's device buffers
+    # warm-up of the host path's own device buffers: a loose tolerance ends
+    # each chunk after one iteration (the solver workspace is already sized)
+    op.gmres_host(b_host, out=x_host, **dict(kw, tol=0.5, maxit=1))
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e2.record(stream)
-    nE = max(1, min(args.steps, 2))
+    nE = 1
     for _ in range(nE):
         op.gmres_host(b_host, out=x_host, **kw)
     e3.record(stream)
@@ -292,24 +295,37 @@ def run_ours(args, wl):
                       "achieved_GBs": round(bmv / (passes[5] * 1e-3) / 1e9, 1),
                       "pass_ms": [round(v, 4) for v in passes[:5]]}
 
-    # FP64 GPU drop-in on one right-hand side (the plain complex128 method)
+    # The plain complex128 GMRES (the drop-in for is_gmres_vie) against the
+    # mixed solver, like for like: both batched over the same first
+    # right-hand sides (one matvec chunk), each timed with CUDA events on the
+    # same operator.  Right-hand sides are solved in chunks one after another
+    # inside a call, so solves/s of one chunk is that of the whole batch.
     fp64 = None
     if not args.skip_fp64:
-        b1 = b[: op.Nb].clone()
+        nb = min(nrhs, tiles["chunk"])
+        bb = b[: nb * op.Nb].clone()
+        f0, f1, f2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         torch.cuda.synchronize()
-        t0 = time.time()
-        x64, rep64 = op.gmres(b1, restart=50, tol=wl["tol"], maxit=200, mode="fp64")
+        f0.record(stream)
+        xm, repm = op.gmres(bb, **kw)
+        f1.record(stream)
+        x64, rep64 = op.gmres(bb, restart=50, tol=wl["tol"], maxit=200, mode="fp64")
+        f2.record(stream)
         torch.cuda.synchronize()
-        dt = time.time() - t0
-        x32 = x[: op.Nb]
-        ferr = float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64))
+        ms_m, ms_64 = f0.elapsed_time(f1), f1.elapsed_time(f2)
+        X32, X64 = xm.reshape(nb, op.Nb), x64.reshape(nb, op.Nb)
+        ferr = (torch.linalg.norm(X32 - X64, dim=1) / torch.linalg.norm(X64, dim=1)).cpu().numpy()
         fp64 = {"operator": "complex128, float-float arithmetic" if op.tiles(0)["float_float"] else "complex128, FP64",
-                "solves_per_s": round(1.0 / dt, 5), "iters": int(rep64.iters[0]),
-                "true_resid": float(rep64.true_resid[0]), "field_err_mixed_vs_fp64": ferr}
+                "batch_rhs": nb, "solves_per_s": round(nb / (ms_64 * 1e-3), 5),
+                "iters_mean": float(np.mean(rep64.iters)), "iters_min_max": [int(rep64.iters.min()), int(rep64.iters.max())],
+                "true_resid_max": float(rep64.true_resid.max()), "converged": int(np.sum(rep64.status == 0)),
+                "mixed_same_batch_solves_per_s": round(nb / (ms_m * 1e-3), 5),
+                "mixed_over_fp64": round(ms_64 / ms_m, 3),
+                "field_err_mixed_vs_fp64_max": float(ferr.max())}
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline(wl, iters=(fp64["iters"] if fp64 else wl["fp64_iters"]), budget_s=args.cpu_budget)
+        cpu = cpu_baseline(wl, iters=(fp64["iters_mean"] if fp64 else wl["fp64_iters"]), budget_s=args.cpu_budget)
     clocks = clk.summary()
     sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
     if sm_mhz:
@@ -336,7 +352,7 @@ def run_ours(args, wl):
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32 accumulation) + FP64 refinement",
             "data": "synthetic (seeded phantom, GPU-assembled Green's tensor, loop incident fields)",
             "config": {"workload": wl["desc"], "grid": [wl["n"]] * 3, "basis": "PWL" if wl["pwl"] else "PWC",
-                       "near_zone": wl.get("near", "standin"),
+                       "near_zone": wl.get("near", "relative"),
                        "n_body_voxels": int(body.idxS.size), "unknowns_per_rhs": int(op.Nb),
                        "rhs_per_gpu": nrhs, "restart": 50, "tol": wl["tol"],
                        "l2": "inputs larger than L2 (Krylov basis and FFT work arrays are tens of GB)",
@@ -410,7 +426,7 @@ def run_matvec_only(args, wl):
     torch.cuda.set_device(0)
     n, res, freq, pwl = wl["n"], wl["res"], wl["freq"], wl["pwl"]
     body = phantoms.ellipsoid_phantom(n, res, seed=0) if wl["phantom"] != "sphere" else phantoms.sphere(n, res)
-    ivN = assemble_green(body.n, res, freq, pwl, "N")
+    ivN = assemble_green(body.n, res, freq, pwl, "N", near=wl.get("near", "relative"))
     prec = {"c64": 2, "c128": 1, "c128ff": 4}[args.prec]
     op = VieOperator(body.n, res, freq, body.idx_solution(pwl), body.Mr(freq), ivN, pwl=pwl, precisions=prec,
                      max_rhs=wl["nrhs"])
@@ -545,9 +561,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     ap.add_argument("--matvec-only", type=int, default=0,
                     help="profiling aid: build the workload, apply mvp_vie this many times, print per-pass times")
-    ap.add_argument("--near", default="standin", choices=["standin", "relative"],
-                    help="near zone of the assembled Green's tensor: the GPU stand-in cubature (default; the "
-                         "measured configuration) or the accurate host cubature with the self point term")
+    ap.add_argument("--near", default="relative", choices=["standin", "relative"],
+                    help="near zone of the assembled Green's tensor: the accurate host cubature that matches the "
+                         "reference's surface-surface near zone (default), or the staggered GPU stand-in cubature")
     ap.add_argument("--prec", default="c64", choices=["c64", "c128", "c128ff"],
                     help="precision of --matvec-only (c128ff: complex128 in float-float arithmetic)")
     args = ap.parse_args()

@@ -327,15 +327,17 @@ class VieOperator:
 
 
 def assemble_green(dims, res, freq, pwl: bool, kernel: str = "N", self_term: str = "pointwise",
-                   near: str = "standin") -> np.ndarray:
+                   near: str = "relative") -> np.ndarray:
     """I_V (n1,n2,n3,pwx,6|3) computed on the GPU (assembly_N.m / assembly_K.m).
 
-    near="relative" replaces the near offsets {0,1}^3 with an accurate host
-    cubature of the same integrals (point term of N included); with
-    near="standin" (the staggered cubature of the GPU kernel),
+    near="relative" (default): the near offsets {0,1}^3 by an accurate host
+    cubature of the same integrals (the point term of N included), equal to
+    the reference's surface-surface near zone with its DIRECTFN singular
+    quadrature (assembly_N.m:56-81) to ~1e-13; far and medium zones by the
+    GPU Gauss rules.  near="standin": the staggered GPU cubature everywhere,
+    which lacks N's point term and is 13% low on face neighbours; with it,
     self_term="distributional" adds the point term of the N kernel at the
-    self offset ((2/3) Gram on the diagonal components; the reference's
-    surface-surface near zone contains it, the stand-in does not)."""
+    self offset ((2/3) Gram on the diagonal components)."""
     if self_term not in ("pointwise", "distributional") or near not in ("standin", "relative"):
         raise ValueError(f"bad self_term {self_term!r} or near {near!r}")
     lib = _lib.load()

@@ -167,9 +167,15 @@ def is_gmres_vie(A, b, restart, tol, maxit, x0, mode="fp64"):
     return (X if was_torch else X.cpu().numpy()), it, resvec
 
 
-def ie_solver_vie(fN: VieOperator, Ue, ce, Mr, Mc, idxS, tol, restart=50, maxit=200, mode="fp64"):
-    """Solver driver of ie_solver_vie.m:14-21 with the port loop batched:
-    rhs = ce * repmat((1./Mr(idxS)).*Mc(idxS), ql, 1) .* Ue(:, i) for all i."""
+def ie_solver_vie(fN: VieOperator, Ue, ce, Mr, Mc, idxS, tol, restart=50, maxit=200, mode="fp64", X=None):
+    """[Jb, U_hat_inv, S_hat_inv, V_hat_inv] = ie_solver_vie(MREDM, gpu_flag)
+    (ie_solver_vie.m:1-32) with the port loop batched:
+    rhs = ce * repmat((1./Mr(idxS)).*Mc(idxS), ql, 1) .* Ue(:, i) for all i,
+    solved from Jb = 0 (:16-21).  ``X`` is MREDM.BASIS.X (N_ports x r) when
+    the excitation basis carries one: then Zbb_hat_inv = X.'*((Ue.'*Jb)*X)
+    (plain transposes) and its economy SVD are returned as (U, S, V) with S
+    diagonal (:23-25), as numpy arrays; otherwise three empty lists (:27-29).
+    Jb follows Ue ((N_b, N_ports); CUDA tensor or numpy)."""
     import torch
     ql = fN.C
     mr = np.asarray(Mr).reshape(-1, order="F")[idxS]
@@ -177,7 +183,16 @@ def ie_solver_vie(fN: VieOperator, Ue, ce, Mr, Mc, idxS, tol, restart=50, maxit=
     chi = np.tile((1.0 / mr) * mc, ql)
     U = _to_cuda(Ue, torch.complex128).reshape(fN.Nb, -1)
     rhs = ce * _to_cuda(chi, torch.complex128)[:, None] * U
-    return is_gmres_vie(fN, rhs, restart, tol, maxit, None, mode=mode)
+    Jb, _it, _rv = is_gmres_vie(fN, rhs, restart, tol, maxit, None, mode=mode)
+    if X is None:
+        return Jb, [], [], []
+    Jd = Jb if isinstance(Jb, torch.Tensor) else _to_cuda(Jb, torch.complex128)
+    Jd = Jd.reshape(fN.Nb, -1)
+    UJ = (U.t() @ Jd).cpu().numpy()                # Ue.' * Jb: N_ports x N_ports
+    Xn = np.asarray(X, dtype=np.complex128)
+    Z = Xn.T @ (UJ @ Xn)
+    Uh, S, Vh = np.linalg.svd(Z, full_matrices=False)
+    return Jb, Uh, np.diag(S), Vh.conj().T
 
 
 def _ports(a, op, dtype):

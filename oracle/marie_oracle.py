@@ -533,6 +533,93 @@ def mvp_op_tucker(Jin: np.ndarray, T: dict, op: str = "N", adjoint: bool = False
     return Jout
 
 
+def _fftn(a, s=None, inverse=False, workers=None):
+    """3D FFT on all host cores where scipy is present (numpy otherwise)."""
+    try:
+        import scipy.fft as sfft
+        f = sfft.ifftn if inverse else sfft.fftn
+        return f(a, s=s, axes=(0, 1, 2), workers=workers or -1)
+    except ImportError:
+        f = np.fft.ifftn if inverse else np.fft.fftn
+        return f(a, s=s, axes=(0, 1, 2))
+
+
+def block_spectrum_dense(IV: np.ndarray, key, kernel: str = "N", workers=None) -> np.ndarray:
+    """Circulant spectrum of block key = (j, k) of a dense I_V
+    (n1, n2, n3, pwx, 6|3): the FFT of the sign-symmetric embedding with the
+    signs of assembly_fft_circ_tucker_{pwc,pwl}.m (G_n*, bt_n*), i.e. the
+    untruncated equivalent of :func:`tucker_block` of
+    :func:`assembly_fft_circ_tucker`."""
+    n1, n2, n3, pwx, nc = IV.shape
+    j, k = key
+    g1, g2, g3 = G_N_SIGNS[nc]
+    b = (BT_SIGNS[0][j], BT_SIGNS[1][j], BT_SIGNS[2][j]) if pwx == 10 else (1, 1, 1)
+    s1, s2, s3 = g1[k] * b[0], g2[k] * b[1], g3[k] * b[2]
+    A3 = IV[:, :, :, j, k]
+    E = np.zeros((2 * n1, 2 * n2, 2 * n3), dtype=complex)
+    ix, jx = np.r_[0:n1, n1 + 1:2 * n1], np.r_[0:n1, n1 - 1:0:-1]
+    iy, jy = np.r_[0:n2, n2 + 1:2 * n2], np.r_[0:n2, n2 - 1:0:-1]
+    iz, jz = np.r_[0:n3, n3 + 1:2 * n3], np.r_[0:n3, n3 - 1:0:-1]
+    sx = np.r_[np.ones(n1), s1 * np.ones(n1 - 1)]
+    sy = np.r_[np.ones(n2), s2 * np.ones(n2 - 1)]
+    sz = np.r_[np.ones(n3), s3 * np.ones(n3 - 1)]
+    E[np.ix_(ix, iy, iz)] = A3[np.ix_(jx, jy, jz)] * sx[:, None, None] * sy[None, :, None] * sz[None, None, :]
+    return _fftn(E, workers=workers)
+
+
+def mvp_op_dense(Jin: np.ndarray, IV: np.ndarray, op: str = "N", adjoint: bool = False,
+                 spectra: dict | None = None, workers=None) -> np.ndarray:
+    """mvp_{N,K}{,_herm_adj}_{pwc,pwl}_tucker.m (the block products of
+    mvp_N_pwl_tucker.m:15-41) with the Green blocks taken untruncated from a
+    dense I_V: each block's spectrum is formed once per call and applied to
+    every (p, q) pair that uses it, so at most one block spectrum is held
+    besides the C input and C output spectra (configuration-size checks:
+    ~3 GB at 96^3, ~7 GB at 128^3 PWL).  ``spectra`` (a dict) keeps the block
+    spectra across calls instead.  FFTs on all host cores."""
+    n1, n2, n3, C = Jin.shape
+    pwl = C == 12
+    m = (2 * n1, 2 * n2, 2 * n3)
+    fJ = [_fftn(Jin[..., q], s=m, workers=workers) for q in range(C)]
+    tab = block_table(op, pwl, adjoint)
+    uses = {}
+    for p in range(C):
+        for q in range(C):
+            e = tab[p][q]
+            if e is not None:
+                uses.setdefault(e[1], []).append((p, q, e[0], e[2]))
+    acc = [np.zeros(m, dtype=complex) for _ in range(C)]
+    for key, lst in uses.items():
+        if spectra is not None and key in spectra:
+            blk = spectra[key]
+        else:
+            blk = block_spectrum_dense(IV, key, op, workers)
+            if spectra is not None:
+                spectra[key] = blk
+        bc = blk.conj() if adjoint else blk
+        for p, q, sg, _cj in lst:
+            if sg > 0:
+                acc[p] += bc * fJ[q]
+            else:
+                acc[p] -= bc * fJ[q]
+        del blk, bc
+    Jout = np.empty(Jin.shape, dtype=complex)
+    for p in range(C):
+        Jout[..., p] = _fftn(acc[p], inverse=True, workers=workers)[:n1, :n2, :n3]
+        acc[p] = None
+    return Jout
+
+
+def mvp_vie_dense(Jb, Mr, Mc, dims, IV, spectra=None, workers=None):
+    """mvp_vie.m:1-19 with the N blocks taken from a dense I_V
+    (:func:`mvp_op_dense`)."""
+    Jp = scatter(Jb, dims)
+    pwl = dims["ql"] == 12
+    NJ = mvp_op_dense(Jp, IV, "N", False, spectra, workers)
+    chi = (1.0 / Mr) * Mc
+    Jout = Jp - chi[..., None] * (invG_scale(pwl, dims["res"])[None, None, None, :] * NJ)
+    return gather(Jout, dims)
+
+
 def invG_scale(pwl: bool, res: float) -> np.ndarray:
     """Per-component diagonal of mvp_invG_pwc.m:3 / mvp_invG_pwl.m:3."""
     if not pwl:
@@ -737,9 +824,12 @@ def vie_rhs(ce, Mr, Mc, idxS, ql, Ue):
     return ce * np.tile(chi, ql) * Ue
 
 
-def ie_solver_vie(Mr, Mc, dims, T, Ue, ce, tol, restart=50, maxit=200):
-    """Restates src/src_solver/src_ie_solver/ie_solver_vie/ie_solver_vie.m:3-21:
-    serial loop over ports with warm start x0 = Jb(:, i) = 0."""
+def ie_solver_vie(Mr, Mc, dims, T, Ue, ce, tol, restart=50, maxit=200, X=None):
+    """Restates src/src_solver/src_ie_solver/ie_solver_vie/ie_solver_vie.m:3-32:
+    serial loop over ports with warm start x0 = Jb(:, i) = 0 (:16-21); with a
+    basis X (MREDM.BASIS.X) also Zbb_hat_inv = X.'*((Ue.'*Jb)*X) and its
+    economy SVD (:23-25; plain transposes, no conjugation).  Returns
+    (Jb, out, (U, S, V)); the factors are None without X (:27-29)."""
     Nports = Ue.shape[1]
     Jb = np.zeros((dims["N_b"], Nports), dtype=complex)
     cache = {}
@@ -750,7 +840,12 @@ def ie_solver_vie(Mr, Mc, dims, T, Ue, ce, tol, restart=50, maxit=200):
         x, it, rv = is_gmres_vie(A, rhs, restart, tol, maxit, Jb[:, i])
         Jb[:, i] = x
         out.append((it, rv))
-    return Jb, out
+    usv = (None, None, None)
+    if X is not None:
+        Z = X.T @ ((Ue.T @ Jb) @ X)
+        U, S, Vh = np.linalg.svd(Z, full_matrices=False)
+        usv = (U, np.diag(S), Vh.conj().T)
+    return Jb, out, usv
 
 
 # ---------------------------------------------------------------------------

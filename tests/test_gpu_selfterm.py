@@ -23,13 +23,13 @@ torch = pytest.importorskip("torch")
 def test_self_point_term_flag(pwl):
     from marie_gb300 import assemble_green
     n, res, freq = (6, 5, 4), 2e-3, 297.2e6
-    a = assemble_green(n, res, freq, pwl, "N")
-    b = assemble_green(n, res, freq, pwl, "N", self_term="distributional")
+    a = assemble_green(n, res, freq, pwl, "N", near="standin")
+    b = assemble_green(n, res, freq, pwl, "N", self_term="distributional", near="standin")
     want = np.zeros_like(a)
     want[0, 0, 0] = O.self_delta_term(res, 10 if pwl else 1)
     assert np.allclose(b - a, want, rtol=0, atol=1e-12 * np.abs(a).max())
-    k0 = assemble_green(n, res, freq, pwl, "K")
-    k1 = assemble_green(n, res, freq, pwl, "K", self_term="distributional")
+    k0 = assemble_green(n, res, freq, pwl, "K", near="standin")
+    k1 = assemble_green(n, res, freq, pwl, "K", self_term="distributional", near="standin")
     assert np.allclose(k1, k0, rtol=0, atol=1e-12 * np.abs(k0).max())
 
 
@@ -38,7 +38,7 @@ def test_self_point_term_flag(pwl):
 def test_near_exact_flag(pwl, kernel):
     from marie_gb300 import assemble_green
     n, res, freq = (5, 4, 3), 2e-3, 297.2e6
-    a = assemble_green(n, res, freq, pwl, kernel)
+    a = assemble_green(n, res, freq, pwl, kernel, near="standin")
     b = assemble_green(n, res, freq, pwl, kernel, near="relative")
     near = [(x, y, z) for x in range(2) for y in range(2) for z in range(2)]
     ref = O.near_zone_relative(O.em_constants(freq)["k0"], res, 10 if pwl else 1, kernel, near)
@@ -73,12 +73,17 @@ def test_quasi_static_sphere_field_gpu():
 @pytest.mark.parametrize("pwl,kernel", [(False, "N"), (True, "N"), (False, "K"), (True, "K")],
                          ids=["pwc-N", "pwl-N", "pwc-K", "pwl-K"])
 def test_gpu_assembly_matches_oracle(pwl, kernel):
-    """marie_assemble_green (far and medium zones by the Gauss rules of
-    assembly_N.m / assembly_K.m, near zone by the stand-in) against the
-    oracle's restatement on the same grid, FP64 both sides."""
+    """The GPU assembly (far and medium zones by the Gauss rules of
+    assembly_N.m / assembly_K.m) against the oracle's restatement on the same
+    grid, FP64 both sides: near zone by the stand-in (marie_assemble_green)
+    and by the accurate cubature (the default of assemble_green, equal to the
+    reference's DIRECTFN surface-surface near zone)."""
     from marie_gb300 import assemble_green
     n, res, freq = (5, 4, 3), 2e-3, 297.2e6
-    got = assemble_green(n, res, freq, pwl, kernel)
-    ref = O.assembly_op(*n, res, O.em_constants(freq)["k0"], pwl, kernel)
-    assert got.shape == ref.shape
-    assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
+    k0 = O.em_constants(freq)["k0"]
+    for near in ("standin", "relative"):
+        got = assemble_green(n, res, freq, pwl, kernel, near=near)
+        ref = O.assembly_op(*n, res, k0, pwl, kernel, near=near)
+        assert got.shape == ref.shape
+        assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max(), near
+    assert np.array_equal(assemble_green(n, res, freq, pwl, kernel), got)

@@ -199,3 +199,22 @@ def test_field_postprocessing_oracle_identities():
     assert rel_err(h(J1 - 3j * J2), h(J1) - 3j * h(J2)) < 1e-13
     phi = O.em_noise_covariance(np.stack([J1, J2, U], 1), P.Mc, ce, P.dims)
     assert np.allclose(phi, phi.conj().T, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
+def test_dense_block_products_equal_tucker_restatement(pwl):
+    """mvp_op_dense (block spectra formed from dense I_V one at a time, the
+    configuration-size checker) equals mvp_op_tucker on a full-rank Tucker
+    form of the same blocks, for N, N^H, K, K^H and mvp_vie."""
+    from helpers import Problem, rel_err
+    P = Problem((6, 5, 4), pwl, seed=3)
+    J = P.random_grid(seed=1)[0]
+    for op, adj in [("N", False), ("N", True), ("K", False), ("K", True)]:
+        IV, T = (P.IV_N, P.TN) if op == "N" else (P.IV_K, P.TK)
+        assert rel_err(O.mvp_op_dense(J, IV, op, adj), O.mvp_op_tucker(J, T, op, adj)) <= 1e-13
+    Jb = P.random_body_vec(seed=2)[0]
+    spectra = {}
+    a = O.mvp_vie_dense(Jb, P.Mr, P.Mc, P.dims, P.IV_N, spectra=spectra)
+    assert len(spectra) == (60 if pwl else 6)
+    assert rel_err(a, O.mvp_vie(Jb, P.Mr, P.Mc, P.dims, P.TN)) <= 1e-13
+    assert rel_err(O.mvp_vie_dense(Jb, P.Mr, P.Mc, P.dims, P.IV_N, spectra=spectra), a) == 0.0
