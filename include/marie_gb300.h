@@ -252,6 +252,52 @@ marie_status marie_vie_gradient(marie_vie* h, const void* J, const void* lam, co
  * complex128, nrhs x N_s. */
 marie_status marie_vie_b1_plus(marie_vie* h, const void* H, int32_t nrhs, void* out, void* stream);
 
+/* Coupled coil/body matvec of the pFFT formulation: Vout =
+ * mvp_svie_pfft(Jcb, pfft_PS, pfft_Z_cc, pfft_Z_bc_N, ext_Mc_inv, func, fN,
+ * Multiplier_1, Multiplier_2, emc, N_sie, res, pfft_dims)
+ * (src/src_solver/src_mvp/mvp_svie/mvp_svie_pfft.m:1-19; its caller
+ * ie_solver_svie_pfft.m:25-27).  Unknowns [Jc; Jb]: n_sie coil currents
+ * then n_b body currents.  grid_op is a marie_vie handle on the extended
+ * (pFFT) grid pfft_n1 x pfft_n2 x pfft_n3 holding its N operator (the
+ * reference's MREDM.operators.pfft_N); it must outlive this handle and not
+ * be an embedded grid.  Sparse matrices are host CSR with 0-based indices
+ * and interleaved complex128 values, copied at create:
+ *   PS     (pfft_n1*pfft_n2*pfft_n3*ql) x (n_sie + n_b)  (pfft_PS)
+ *   Z_cc   n_sie x n_sie                                 (pfft_Z_cc)
+ *   Z_bc_N n_b x n_sie                                   (pfft_Z_bc_N)
+ * ext_Mc_inv: host, pfft_n1*pfft_n2*pfft_n3 complex128 (EP.ext_Mc_inv,
+ * em_assembly.m:35-37).  M1 / M2: host, n_sie + n_b doubles, or NULL for
+ * ie_solver_svie_pfft.m's [ones(N_sie); -ones(N_b)] and [zeros(N_sie);
+ * ones(N_b)]. */
+typedef struct {
+  int64_t rows, cols, nnz;
+  const int64_t* row_ptr;   /* rows + 1 */
+  const int64_t* col_idx;   /* nnz */
+  const double* val;        /* 2 * nnz (re, im) */
+} marie_csr;
+
+typedef struct marie_svie_pfft marie_svie_pfft; /* opaque handle */
+
+typedef struct {
+  marie_vie* grid_op;
+  int64_t n_sie;
+  int64_t n_b;
+  marie_csr PS;
+  marie_csr Z_cc;
+  marie_csr Z_bc_N;
+  const double* ext_Mc_inv;
+  const double* M1;
+  const double* M2;
+} marie_svie_pfft_desc;
+
+marie_status marie_svie_pfft_create(marie_svie_pfft** h, const marie_svie_pfft_desc* d);
+/* y = mvp_svie_pfft(x) for nrhs right-hand sides (device, nrhs x (n_sie +
+ * n_b), precision prec; complex64 needs the grid handle's complex64 state,
+ * complex128 its complex128 or float-float state), on `stream`. */
+marie_status marie_svie_pfft_apply(marie_svie_pfft* h, int32_t prec, const void* x, void* y, int32_t nrhs,
+                                   void* stream);
+marie_status marie_svie_pfft_destroy(marie_svie_pfft* h);
+
 /* Diagnostics. */
 /* Average device time [ms] of each matvec pass over `reps` repetitions of
  * one mvp_vie application of nrhs right-hand sides (x/y: device, precision

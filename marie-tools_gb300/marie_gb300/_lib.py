@@ -60,8 +60,22 @@ class GmresReport(ct.Structure):
                 ("matvecs_c128", ct.c_int32), ("matvecs_c64", ct.c_int32)]
 
 
+class Csr(ct.Structure):
+    _fields_ = [("rows", ct.c_int64), ("cols", ct.c_int64), ("nnz", ct.c_int64),
+                ("row_ptr", ct.POINTER(ct.c_int64)), ("col_idx", ct.POINTER(ct.c_int64)), ("val", c_double_p)]
+
+
+class SviePfftDesc(ct.Structure):
+    _fields_ = [("grid_op", ct.c_void_p), ("n_sie", ct.c_int64), ("n_b", ct.c_int64), ("PS", Csr),
+                ("Z_cc", Csr), ("Z_bc_N", Csr), ("ext_Mc_inv", c_double_p), ("M1", c_double_p),
+                ("M2", c_double_p)]
+
+
 _vp = ct.c_void_p
 _PROTOS = {
+    "marie_svie_pfft_create": (ct.c_int, [ct.POINTER(_vp), ct.POINTER(SviePfftDesc)]),
+    "marie_svie_pfft_apply": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, _vp]),
+    "marie_svie_pfft_destroy": (ct.c_int, [_vp]),
     "marie_vie_create": (ct.c_int, [ct.POINTER(_vp), ct.POINTER(VieDesc)]),
     "marie_vie_destroy": (ct.c_int, [_vp]),
     "marie_vie_apply": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, _vp]),

@@ -849,6 +849,37 @@ def ie_solver_vie(Mr, Mc, dims, T, Ue, ce, tol, restart=50, maxit=200, X=None):
 
 
 # ---------------------------------------------------------------------------
+# Coupled coil/body matvec of the pFFT formulation
+# ---------------------------------------------------------------------------
+
+
+def mvp_svie_pfft(Jcb, PS, Z_cc, Z_bc_N, ext_Mc_inv, T, M1, M2, ce, N_sie, res, pfft_dims, cache=None):
+    """Restates src/src_solver/src_mvp/mvp_svie/mvp_svie_pfft.m:1-19 (scipy
+    sparse PS / Z_cc / Z_bc_N; ``T`` the extended grid's N operator as
+    Tucker blocks, or a dense I_V array; ``.'`` is the plain transpose):
+      Jb = PS [0; Jcb(N_sie+1:end)], Jtot = PS Jcb              (:4-5)
+      Jout_1 = 1/ce M1 .* (PS.' (mvp_N(Jtot) - mvp_G(Jtot)))    (:8-9)
+      Jout_2 = 1/ce M2 .* (PS.' mvp_G(ext_Mc_inv .* Jb))        (:11-12)
+      Jout_3 = [Z_cc Jc + Z_bc_N.' Jb; -Z_bc_N Jc]              (:14)"""
+    dims = tuple(int(v) for v in pfft_dims)
+    pwl = dims[3] == 12
+    Jc, Jbv = Jcb[:N_sie], Jcb[N_sie:]
+    Jb = (PS @ np.concatenate([np.zeros(N_sie, dtype=complex), Jbv])).reshape(dims, order="F")
+    Jtot = (PS @ Jcb).reshape(dims, order="F")
+    Gd = G_scale(pwl, res)[None, None, None, :]
+    if isinstance(T, dict):
+        NJ = mvp_op_tucker(Jtot, T, "N", False, cache)
+    else:
+        NJ = mvp_op_dense(Jtot, T, "N", False, cache)
+    J1 = NJ - Gd * Jtot
+    out1 = (1.0 / ce) * M1 * (PS.T @ J1.reshape(-1, order="F"))
+    J2 = Gd * (np.asarray(ext_Mc_inv)[..., None] * Jb)
+    out2 = (1.0 / ce) * M2 * (PS.T @ J2.reshape(-1, order="F"))
+    out3 = np.concatenate([Z_cc @ Jc + Z_bc_N.T @ Jbv, -(Z_bc_N @ Jc)])
+    return out1 + out2 + out3
+
+
+# ---------------------------------------------------------------------------
 # Incident fields tested onto the PWC/PWL basis
 # ---------------------------------------------------------------------------
 

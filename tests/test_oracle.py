@@ -218,3 +218,41 @@ def test_dense_block_products_equal_tucker_restatement(pwl):
     assert len(spectra) == (60 if pwl else 6)
     assert rel_err(a, O.mvp_vie(Jb, P.Mr, P.Mc, P.dims, P.TN)) <= 1e-13
     assert rel_err(O.mvp_vie_dense(Jb, P.Mr, P.Mc, P.dims, P.IV_N, spectra=spectra), a) == 0.0
+
+
+def test_mvp_svie_pfft_restatement_against_dense_matrices():
+    """oracle.mvp_svie_pfft (mvp_svie_pfft.m:1-19) against the same formula
+    written with dense matrices on a 3 x 3 x 2 PWC extended grid: N as the
+    matrix of mvp_N on the grid's unit vectors, G as the Gram diagonal."""
+    import scipy.sparse as sp
+    from helpers import synthetic_IV, rel_err
+    rng = np.random.default_rng(0)
+    n, ql, n_sie, res, ce = (3, 3, 2), 3, 4, 5e-3, 1j * 0.01
+    nvox = 18
+    ng = nvox * ql
+    idxS = np.array([4, 5, 13])
+    N_b = ql * idxS.size
+    IV = synthetic_IV(n, False, "N", 3)
+    Nmat = np.zeros((ng, ng), complex)
+    for j in range(ng):
+        e = np.zeros(ng, complex)
+        e[j] = 1
+        Nmat[:, j] = O.mvp_op_dense(e.reshape(n + (ql,), order="F"), IV, "N").reshape(-1, order="F")
+    PSd = np.zeros((ng, n_sie + N_b), complex)
+    PSd[np.concatenate([c * nvox + idxS for c in range(ql)]), n_sie + np.arange(N_b)] = 1
+    PSd[:, :n_sie] = (rng.uniform(size=(ng, n_sie)) < 0.2) * (rng.normal(size=(ng, n_sie)) + 1j)
+    Zcc = rng.normal(size=(n_sie, n_sie)) + 1j * rng.normal(size=(n_sie, n_sie))
+    Zbc = rng.normal(size=(N_b, n_sie)) + 1j * rng.normal(size=(N_b, n_sie))
+    mc = np.zeros(n, complex)
+    mc.reshape(-1, order="F")[idxS] = rng.normal(size=idxS.size) + 1j * rng.normal(size=idxS.size)
+    M1 = np.r_[np.ones(n_sie), -np.ones(N_b)]
+    M2 = np.r_[np.zeros(n_sie), np.ones(N_b)]
+    x = rng.normal(size=n_sie + N_b) + 1j * rng.normal(size=n_sie + N_b)
+    got = O.mvp_svie_pfft(x, sp.csr_matrix(PSd), sp.csr_matrix(Zcc), sp.csr_matrix(Zbc), mc, IV, M1, M2, ce,
+                          n_sie, res, n + (ql,))
+    G = res ** 3 * np.eye(ng)
+    Mcd = np.diag(np.tile(mc.reshape(-1, order="F"), ql))
+    xb = np.r_[np.zeros(n_sie), x[n_sie:]]
+    want = (M1 * (PSd.T @ ((Nmat - G) @ (PSd @ x))) + M2 * (PSd.T @ (G @ (Mcd @ (PSd @ xb))))) / ce
+    want += np.r_[Zcc @ x[:n_sie] + Zbc.T @ x[n_sie:], -(Zbc @ x[:n_sie])]
+    assert rel_err(got, want) <= 1e-13
