@@ -211,6 +211,22 @@ marie_status marie_assemble_green_ex(int32_t n1, int32_t n2, int32_t n3, double 
  * complex128, nloop x N_b.  voxel centres: centre of voxel (0,0,0) = origin. */
 marie_status marie_incident_loops(marie_vie* h, const double* origin, const double* loops, int32_t nloop,
                                   double radius, int32_t nseg, void* out_dev, void* stream);
+/* Incident field of wire currents in the reference's wire-basis convention,
+ * as coefficients on the body: invG(Zbw * coef) restricted to the body, with
+ * Zbw the voxel-wire coupling of Assemble_tri_coupling_matrix_N_* (kind 0,
+ * electric field) or _K_* (kind 1, magnetic field) times res^3
+ * (src_wvie/Cpp_Assembly/src/Assemble_tri_coupling_matrix_N_x.cpp:21-205,
+ * wvie_mrgf_assembly.m:26-49; the tested fields of em_efield_wvie.m:43-47 and
+ * em_hfield_wvie.m:38).  Wire basis t spans r_p -> r_2 -> r_n (host, n_tri x 3
+ * doubles each); both halves carry a current ramping up from the half's start
+ * point, as the reference places its source points.  coef: host, nrhs x n_tri
+ * complex128 wire currents, or NULL for all ones (a closed loop of unit
+ * coefficients).  q_wire / q_vox: Gauss points per half / per voxel axis
+ * (the reference's Quad_order_wie_coup = 4, Quad_order_vie = 2).  out: device
+ * complex128, nrhs x N_b. */
+marie_status marie_incident_wire(marie_vie* h, int32_t kind, const double* origin, const double* r_p,
+                                 const double* r_n, const double* r_2, int32_t n_tri, const double* coef,
+                                 int32_t nrhs, int32_t q_wire, int32_t q_vox, void* out_dev, void* stream);
 /* Unit x-polarised plane wave exp(-i k0 z) tested onto the basis. */
 marie_status marie_incident_plane_wave(marie_vie* h, const double* origin, void* out_dev, void* stream);
 

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(128) k_vv(const int* offs, const int* rule_of,
   }
 }
 
-static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
   // Newton iteration on P_n; nodes ascending.
   x.assign(n, 0.0);
   w.assign(n, 0.0);

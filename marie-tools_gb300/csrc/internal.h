@@ -136,6 +136,9 @@ marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaS
 
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
 
+// n-point Gauss-Legendre rule on [-1, 1], nodes ascending (host).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
+
 // Largest dynamic shared memory a CTA may opt into on sm_100-family GPUs.
 constexpr size_t kSmemOptin = 227 * 1024;
 

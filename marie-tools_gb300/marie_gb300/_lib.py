@@ -95,6 +95,8 @@ _PROTOS = {
     "marie_incident_loops": (ct.c_int, [_vp, c_double_p, c_double_p, ct.c_int32, ct.c_double,
                                         ct.c_int32, _vp, _vp]),
     "marie_incident_plane_wave": (ct.c_int, [_vp, c_double_p, _vp, _vp]),
+    "marie_incident_wire": (ct.c_int, [_vp, ct.c_int32, c_double_p, c_double_p, c_double_p, c_double_p, ct.c_int32,
+                                       c_double_p, ct.c_int32, ct.c_int32, ct.c_int32, _vp, _vp]),
     "marie_vie_apply_N_noalloc": (ct.c_int, [ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, _vp, _vp, _vp,
                                              _vp]),
     "marie_vie_profile": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, ct.c_int32, c_double_p, _vp]),

@@ -317,6 +317,28 @@ class VieOperator:
                                              int(nseg), ct.c_void_p(out.data_ptr()), self._stream()))
         return out
 
+    def incident_wire(self, origin, r_p, r_n, r_2, coef=None, *, kind="E", q_wire=4, q_vox=2):
+        """Incident E (kind "E") or H (kind "H") field coefficients on the body
+        of wire currents in the reference's wire-basis convention
+        (Assemble_tri_coupling_matrix_{N,K}_*.cpp, wvie_mrgf_assembly.m):
+        r_p / r_n / r_2 (n_tri, 3) basis nodes, coef (nrhs, n_tri) complex wire
+        currents or None for all ones.  Returns (nrhs*N_b) complex128 CUDA."""
+        import torch
+        pts = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, 3)) for a in (r_p, r_n, r_2)]
+        ntri = pts[0].shape[0]
+        if coef is None:
+            cf, nrhs = None, 1
+        else:
+            c = np.ascontiguousarray(np.asarray(coef, dtype=np.complex128).reshape(-1, ntri))
+            nrhs = c.shape[0]
+            cf = c.view(np.float64)
+        org = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))
+        out = torch.empty(nrhs * self.Nb, dtype=torch.complex128, device="cuda")
+        check(self._lib.marie_incident_wire(self._h, 0 if kind == "E" else 1, _dptr(org), *(_dptr(a) for a in pts),
+                                            ntri, None if cf is None else _dptr(cf), nrhs, int(q_wire), int(q_vox),
+                                            ct.c_void_p(out.data_ptr()), self._stream()))
+        return out
+
     def incident_plane_wave(self, origin):
         import torch
         org = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))

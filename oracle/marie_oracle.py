@@ -943,6 +943,90 @@ def loop_field(points, mid, dl, k0, omega, mu0, current=1.0):
     return -1j * omega * mu0 * current * E
 
 
+def wire_sources(r_p, r_n, r_2, q_wire=4):
+    """Quadrature points of the wire triangle bases as
+    Assemble_tri_coupling_matrix_*.cpp (get_source_coords_mat, its :214-238)
+    places them: for basis i, the positive half runs r_p -> r_2 and the
+    negative half r_2 -> r_n; on each half, Gauss point s = L/2 (x + 1) from
+    the half's start carries the current (s/L) * (unit tangent), i.e. both
+    halves ramp up from their start point.  Returns (points (N_tri, 2, q, 3),
+    current vectors (N_tri, 2, q, 3), weights w_i * L/2 (N_tri, 2, q))."""
+    w, x = gauss_1d(q_wire)
+    r_p, r_n, r_2 = (np.asarray(a, float).reshape(-1, 3) for a in (r_p, r_n, r_2))
+    pts, cur, wts = [], [], []
+    for a, b in ((r_p, r_2), (r_2, r_n)):
+        d = b - a
+        L = np.linalg.norm(d, axis=1)
+        frac = 0.5 * (x + 1.0)                                   # s / L
+        pts.append(a[:, None, :] + frac[None, :, None] * d[:, None, :])
+        cur.append(frac[None, :, None] * (d / L[:, None])[:, None, :])
+        wts.append(w[None, :] * (L / 2.0)[:, None])
+    return np.stack(pts, 1), np.stack(cur, 1), np.stack(wts, 1)
+
+
+def wire_coupling(kind, centres, r_p, r_n, r_2, res, k0, pwl, q_wire=4, q_vox=2):
+    """Restates Assemble_tri_coupling_matrix_{N,K}_{x,x1,x2,x3,y,...,z3}.cpp
+    (src/src_integral_equations/src_wvie/Cpp_Assembly/src, :21-205) times
+    res^3 as wvie_mrgf_assembly.m:26-49 applies it: the voxel integral of
+    each field component (and, PWL, of its products with the moments
+    f = x/2, y/2, z/2 of the voxel's local coordinates in [-1, 1]) of the
+    current of each wire basis; kind "N": the electric field by the full
+    dyadic kernel, scaled by -1/(4 pi ce), ce = i k0 c0 e0; kind "K": the
+    magnetic field G (R x t), G = e^{-i k0 R} (1 + i k0 R) / R^3 * (-1/4pi).
+    Gauss rules q_vox^3 per voxel, q_wire per half (Quad_order_vie = 2,
+    Quad_order_wie_coup = 4, load_inputs.m:81-83).  Returns (ql, N_vox,
+    N_tri) in the reference's component order (x, x1, x2, x3, y, ... for
+    PWL)."""
+    wv, xv = gauss_1d(q_vox)
+    spts, scur, swts = wire_sources(r_p, r_n, r_2, q_wire)
+    ntri = spts.shape[0]
+    c = np.asarray(centres, float).reshape(-1, 3)
+    nv = c.shape[0]
+    L = 4 if pwl else 1
+    mu0, c0 = 4e-7 * math.pi, 299792458.0
+    e0 = 1.0 / (c0 * c0 * mu0)
+    ce = 1j * k0 * c0 * e0
+    out = np.zeros((3, L, nv, ntri), dtype=complex)
+    S = spts.reshape(ntri, -1, 3)
+    Tc = scur.reshape(ntri, -1, 3)
+    W = swts.reshape(ntri, -1)
+    for a in range(q_vox):
+        for b in range(q_vox):
+            for cc in range(q_vox):
+                loc = np.array([xv[a], xv[b], xv[cc]])
+                wt = wv[a] * wv[b] * wv[cc] / 8.0
+                obs = c + 0.5 * res * loc[None, :]
+                R = obs[:, None, None, :] - S[None, :, :, :]          # (nv, ntri, nsrc, 3)
+                Rd = np.linalg.norm(R, axis=-1)
+                kR = k0 * Rd
+                kappa = np.exp(-1j * kR) / Rd ** 3
+                if kind == "N":
+                    P = (kR ** 2 - 3j * kR - 3.0) / Rd ** 2
+                    Q = (kR ** 2 - 1j * kR - 1.0) / P
+                    Rt = np.sum(R * Tc[None], axis=-1)
+                    F = (kappa * P)[..., None] * (R * Rt[..., None] - Q[..., None] * Tc[None])
+                    F = F * (-1.0 / ce / (4 * math.pi))
+                else:
+                    G = kappa * (1j * kR + 1.0) * (-1.0 / (4 * math.pi))
+                    F = G[..., None] * np.cross(R, np.broadcast_to(Tc[None], R.shape))
+                fld = np.sum(F * W[None, :, :, None], axis=2)          # (nv, ntri, 3)
+                fl = [1.0, 0.5 * loc[0], 0.5 * loc[1], 0.5 * loc[2]]
+                for p in range(3):
+                    for l in range(L):
+                        out[p, l] += wt * fl[l] * fld[:, :, p]
+    return out.reshape(3 * L, nv, ntri) * res ** 3
+
+
+def wire_incident(kind, centres, r_p, r_n, r_2, coef, res, k0, pwl, q_wire=4, q_vox=2):
+    """Incident field coefficients on the body of wire currents ``coef``
+    (N_tri,): invG(Zbw coef) (the tested field of em_efield_wvie.m:43-47 /
+    em_hfield_wvie.m:38, restricted to the body), component-major (N_b,)."""
+    Z = wire_coupling(kind, centres, r_p, r_n, r_2, res, k0, pwl, q_wire, q_vox)
+    t = Z @ np.asarray(coef, dtype=complex)
+    g = invG_scale(pwl, res)
+    return (t * g[:, None]).reshape(-1)
+
+
 def plane_wave_field(points, k0):
     """E = x_hat * exp(-i k0 z): unit x-polarised plane wave along +z."""
     E = np.zeros((points.shape[0], 3), dtype=complex)

@@ -1,6 +1,6 @@
 """The reference's wire-to-voxel coupling kernels, compiled from its sources
-(oracle/Makefile -> oracle/_ref/libtri_N_{x,y,z}.so), for the checks of the
-loop right-hand sides.
+(oracle/Makefile -> oracle/_ref/libtri_{N,K}_{x,x1,...,z3}.so), for the
+checks of the loop and wire right-hand sides.
 
 TEST INFRASTRUCTURE ONLY.
 
@@ -27,27 +27,29 @@ _D = ct.POINTER(ct.c_double)
 _libs = {}
 
 
-def load(v):
-    if v not in _libs:
-        path = Path(__file__).resolve().parent / "_ref" / f"libtri_N_{v}.so"
+def load(v, kind="N"):
+    key = f"{kind}_{v}"
+    if key not in _libs:
+        path = Path(__file__).resolve().parent / "_ref" / f"libtri_{key}.so"
         if not path.exists():
             raise FileNotFoundError(f"{path} not built (make -C oracle REF=<reference checkout>)")
         lib = ct.CDLL(str(path))
         lib.oracle_tri_coupling.argtypes = [_D] * 7 + [ct.c_double, ct.c_size_t, ct.c_size_t, ct.c_double]
-        _libs[v] = lib
-    return _libs[v]
+        _libs[key] = lib
+    return _libs[key]
 
 
-def tri_coupling(v, centres, r_p, r_n, r_2, res, k0, q_wire=4, q_vox=2):
-    """(N_vox, N_tri) coupling of component v ('x', 'y', 'z'); centres and the
-    r_* arrays are (N, 3)."""
+def tri_coupling(v, centres, r_p, r_n, r_2, res, k0, q_wire=4, q_vox=2, kind="N"):
+    """(N_vox, N_tri) coupling of component v ('x', 'x1', ..., 'z3') of the
+    electric (kind "N") or magnetic (kind "K") field; centres and the r_*
+    arrays are (N, 3).  Without the res^3 of wvie_mrgf_assembly.m."""
     w, x = O.gauss_1d(q_wire)
     wq = np.ascontiguousarray(np.r_[q_wire, w, x], dtype=float)
     w, x = O.gauss_1d(q_vox)
     vq = np.ascontiguousarray(np.r_[q_vox, w, x], dtype=float)
     arrs = [np.ascontiguousarray(a, dtype=float) for a in (centres, r_p, r_n, r_2)]
     Z = np.zeros(2 * len(arrs[0]) * len(arrs[1]))
-    load(v).oracle_tri_coupling(Z.ctypes.data_as(_D), *[a.ctypes.data_as(_D) for a in arrs], wq.ctypes.data_as(_D),
+    load(v, kind).oracle_tri_coupling(Z.ctypes.data_as(_D), *[a.ctypes.data_as(_D) for a in arrs], wq.ctypes.data_as(_D),
                                 vq.ctypes.data_as(_D), res, len(arrs[0]), len(arrs[1]), k0)
     return Z.view(np.complex128).reshape((len(arrs[0]), len(arrs[1])), order="F")
 

@@ -92,3 +92,44 @@ def test_loop_full_size_phantom_sampled():
                         freq)[0].reshape(12, -1)
     assert rel_err(got.reshape(12, Ns)[:, pick], ref) <= TOL
     op.close()
+
+
+def _loop_bases(centre, normal, radius, nseg):
+    """Triangle bases of a closed regular nseg-gon: basis i spans nodes
+    i-1 -> i -> i+1 (the wire layout of a closed loop)."""
+    normal = np.asarray(normal, float) / np.linalg.norm(normal)
+    a = np.array([1.0, 0, 0]) if abs(normal[0]) < 0.9 else np.array([0, 1.0, 0])
+    e1 = np.cross(normal, a)
+    e1 /= np.linalg.norm(e1)
+    e2 = np.cross(normal, e1)
+    t = 2 * np.pi * np.arange(nseg) / nseg
+    P = np.asarray(centre, float)[None, :] + radius * (np.cos(t)[:, None] * e1 + np.sin(t)[:, None] * e2)
+    return np.roll(P, 1, axis=0), np.roll(P, -1, axis=0), P
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pwl", [False, True], ids=["pwc", "pwl"])
+def test_wire_fields_match_oracle(pwl):
+    """marie_incident_wire (E and H, unit and complex wire currents, two
+    right-hand sides) against oracle.wire_incident, the restatement of the
+    reference's Assemble_tri_coupling_matrix_{N,K}_* kernels (which
+    tests/test_loop_field_reference.py pins to those kernels compiled from
+    source)."""
+    from marie_gb300 import phantoms
+    n, res, freq = 24, 2e-3, 297.2e6
+    body = phantoms.ellipsoid_phantom(n, res, seed=2, scale=0.25)
+    k0 = O.em_constants(freq)["k0"]
+    op = _op(body, res, freq, pwl, 2)
+    r_p, r_n, r_2 = _loop_bases([0.0, 0.0, 0.04], [0.1, 0.0, 1.0], 0.02, 16)
+    rng = np.random.default_rng(7)
+    coef = rng.normal(size=(2, 16)) + 1j * rng.normal(size=(2, 16))
+    cen = _centres(body, res)
+    for kind, kk in (("E", "N"), ("H", "K")):
+        got = op.incident_wire(body.origin, r_p, r_n, r_2, kind=kind).cpu().numpy()
+        ref = O.wire_incident(kk, cen, r_p, r_n, r_2, np.ones(16), res, k0, pwl)
+        assert rel_err(got, ref) <= TOL, kind
+        got2 = op.incident_wire(body.origin, r_p, r_n, r_2, coef, kind=kind).cpu().numpy().reshape(2, -1)
+        for r in range(2):
+            ref2 = O.wire_incident(kk, cen, r_p, r_n, r_2, coef[r], res, k0, pwl)
+            assert rel_err(got2[r], ref2) <= TOL, (kind, r)
+    op.close()
