@@ -176,6 +176,15 @@ marie_status marie_gmres_vie(marie_vie* h, const void* b, void* x, int32_t nrhs,
 marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, void* x_host, int32_t nrhs,
                                   const marie_gmres_opts* opts, marie_gmres_report* report, void* stream);
 
+/* Replaces the body's materials: Mr_body (host, N_s complex128, body voxels
+ * in idx_solution order) = eps_r + sigma/ce per voxel (em_assembly.m:14).
+ * Recomputes the contrast (1./Mr).*Mc of every built precision and the
+ * absorbed-power weights; the Green's tensor, body map and workspaces stay.
+ * Waits for the device to be idle first.  No counterpart in the reference
+ * (which rebuilds EP); used by material sweeps and finite-difference checks
+ * of the adjoint gradient. */
+marie_status marie_vie_set_materials(marie_vie* h, const double* Mr_body);
+
 /* Frees the GMRES workspace the handle keeps between solves (Krylov basis,
  * residual vectors; reused by the next solve of the same or smaller shape).
  * No counterpart in the reference (MATLAB frees its arrays itself). */

@@ -484,6 +484,45 @@ template marie_status launch_matvec<float>(marie_vie*, int, int, const cplx<floa
 template marie_status launch_matvec<double>(marie_vie*, int, int, const cplx<double>*, int64_t, cplx<double>*,
                                             int64_t, int, const unsigned char*, cudaStream_t);
 
+// Body-voxel material data from Mr per body voxel: the contrast
+// chi = (1./Mr).*Mc (mvp_vie.m:17), the absorbed-power weight
+// real(Mc_inv/ce) (em_ehfield_vie.m:46; 0 where Mc = 0) and Mr itself.
+static marie_status body_materials(const marie_vie* h, const std::complex<double>* mr, std::vector<cplx<double>>& chi,
+                                   std::vector<double>& wpow, std::vector<cplx<double>>& mrb) {
+  chi.resize(h->Ns);
+  wpow.resize(h->Ns);
+  mrb.resize(h->Ns);
+  for (int64_t s = 0; s < h->Ns; ++s) {
+    const std::complex<double> Mr = mr[s];
+    if (!std::isfinite(Mr.real()) || !std::isfinite(Mr.imag()) || Mr == 0.0) {
+      set_error("Mr is zero or non-finite at body voxel %lld", (long long)s);
+      return MARIE_ERR_NONFINITE;
+    }
+    const std::complex<double> Mc = Mr - 1.0;
+    const std::complex<double> v = (1.0 / Mr) * Mc;
+    chi[s] = cplx<double>{v.real(), v.imag()};
+    wpow[s] = Mc == 0.0 ? 0.0 : ((1.0 / Mc) / std::complex<double>(0.0, h->ce_im)).real();
+    mrb[s] = cplx<double>{Mr.real(), Mr.imag()};
+  }
+  return MARIE_OK;
+}
+
+// Upload the contrast of every built precision (create and material updates).
+static marie_status upload_chi(marie_vie* h, const std::vector<cplx<double>>& chi) {
+  if (h->p64.chi) MARIE_CUDA_TRY(cudaMemcpy(h->p64.chi, chi.data(), h->Ns * sizeof(cplx<double>), cudaMemcpyHostToDevice));
+  if (h->p32.chi) {
+    std::vector<cplx<float>> f(h->Ns);
+    for (int64_t s = 0; s < h->Ns; ++s) f[s] = cplx<float>{(float)chi[s].x, (float)chi[s].y};
+    MARIE_CUDA_TRY(cudaMemcpy(h->p32.chi, f.data(), h->Ns * sizeof(cplx<float>), cudaMemcpyHostToDevice));
+  }
+  if (h->pff.chi) {
+    std::vector<cplx<ff>> f(h->Ns);
+    for (int64_t s = 0; s < h->Ns; ++s) f[s] = cplx<ff>{prec_from<ff>(chi[s].x), prec_from<ff>(chi[s].y)};
+    MARIE_CUDA_TRY(cudaMemcpy(h->pff.chi, f.data(), h->Ns * sizeof(cplx<ff>), cudaMemcpyHostToDevice));
+  }
+  return MARIE_OK;
+}
+
 }  // namespace marie
 
 using namespace marie;
@@ -619,21 +658,13 @@ static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
   if ((st = dev_alloc(h, (void**)&h->idxS, h->Ns * sizeof(int64_t))) != MARIE_OK) return fail(st);
   cudaMemcpy(h->idxS, idxS.data(), h->Ns * sizeof(int64_t), cudaMemcpyHostToDevice);
   // contrast chi = (1./Mr).*Mc on the body (mvp_vie.m:17)
-  std::vector<cplx<double>> chi(h->Ns);
-  std::vector<double> wpow(h->Ns);
-  std::vector<cplx<double>> mrb(h->Ns);
-  for (int64_t s = 0; s < h->Ns; ++s) {
-    const std::complex<double> Mr(d->Mr[2 * idxS[s]], d->Mr[2 * idxS[s] + 1]);
-    if (!std::isfinite(Mr.real()) || !std::isfinite(Mr.imag()) || Mr == 0.0) {
-      set_error("Mr is zero or non-finite at body voxel %lld", (long long)s);
-      return fail(MARIE_ERR_NONFINITE);
-    }
-    const std::complex<double> Mc = Mr - 1.0;
-    const std::complex<double> v = (1.0 / Mr) * Mc;
-    chi[s] = cplx<double>{v.real(), v.imag()};
-    // real(Mc_inv / ce), the absorbed-power weight of em_ehfield_vie.m:46 (0 where Mc = 0)
-    wpow[s] = Mc == 0.0 ? 0.0 : ((1.0 / Mc) / std::complex<double>(0.0, h->ce_im)).real();
-    mrb[s] = cplx<double>{Mr.real(), Mr.imag()};
+  std::vector<cplx<double>> chi;
+  std::vector<double> wpow;
+  std::vector<cplx<double>> mrb;
+  {
+    std::vector<std::complex<double>> mr(h->Ns);
+    for (int64_t s = 0; s < h->Ns; ++s) mr[s] = {d->Mr[2 * idxS[s]], d->Mr[2 * idxS[s] + 1]};
+    if ((st = body_materials(h, mr.data(), chi, wpow, mrb)) != MARIE_OK) return fail(st);
   }
   if ((st = dev_alloc(h, (void**)&h->mr_body, h->Ns * sizeof(cplx<double>))) != MARIE_OK) return fail(st);
   cudaMemcpy(h->mr_body, mrb.data(), h->Ns * sizeof(cplx<double>), cudaMemcpyHostToDevice);
@@ -713,6 +744,20 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   (*out)->on1 = n[0];
   (*out)->on2 = n[1];
   (*out)->on3 = n[2];
+  return MARIE_OK;
+}
+
+marie_status marie_vie_set_materials(marie_vie* h, const double* Mr_body) {
+  if (!h || !Mr_body) { set_error("set_materials: NULL argument"); return MARIE_ERR_BAD_ARG; }
+  std::vector<std::complex<double>> mr(h->Ns);
+  for (int64_t s = 0; s < h->Ns; ++s) mr[s] = {Mr_body[2 * s], Mr_body[2 * s + 1]};
+  std::vector<cplx<double>> chi, mrb;
+  std::vector<double> wpow;
+  MARIE_TRY(body_materials(h, mr.data(), chi, wpow, mrb));
+  MARIE_CUDA_TRY(cudaDeviceSynchronize());   // no kernel may still read the old values
+  MARIE_TRY(upload_chi(h, chi));
+  MARIE_CUDA_TRY(cudaMemcpy(h->wpow, wpow.data(), h->Ns * sizeof(double), cudaMemcpyHostToDevice));
+  MARIE_CUDA_TRY(cudaMemcpy(h->mr_body, mrb.data(), h->Ns * sizeof(cplx<double>), cudaMemcpyHostToDevice));
   return MARIE_OK;
 }
 

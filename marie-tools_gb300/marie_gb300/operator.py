@@ -115,6 +115,14 @@ class VieOperator:
         """Free the GMRES workspace kept between solves."""
         check(self._lib.marie_vie_release_workspace(self._h))
 
+    def set_materials(self, Mr_body):
+        """Replace the body's Mr = eps_r + sigma/ce (N_s complex values, body
+        voxels in idx_solution order); the Green's tensor stays."""
+        mr = np.ascontiguousarray(np.asarray(Mr_body, dtype=np.complex128).reshape(-1))
+        if mr.size != self.Ns:
+            raise ValueError(f"Mr_body must have N_s = {self.Ns} entries")
+        check(self._lib.marie_vie_set_materials(self._h, _dptr(mr.view(np.float64))))
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.marie_vie_destroy(self._h)

@@ -249,17 +249,21 @@ def b1_objective(op: VieOperator, J, Ue, Ub, roi):
     return M / P, M, P, E, H, b1
 
 
-def b1_objective_gradient(op: VieOperator, b, Ue, Ub, roi, *, tol=1e-6, mode="mixed", J=None):
+def b1_objective_gradient(op: VieOperator, b, Ue, Ub, roi, *, tol=1e-6, mode="mixed", J=None, solve_op=None):
     """Adjoint gradient of J_obj = mean_ROI |B1+|^2 / P_abs with respect to
     eps_r and sigma of every body voxel, for the solution J of A J = b (one
     right-hand side; J is solved here unless given).  Steps: forward solve,
     fields, B1+ and P; adjoint source g = dJ_obj/dconj(J) (the B1+ part
     through marie_vie_apply_hfield_adjoint); adjoint solve A^H lam = g;
-    per-voxel sensitivities (marie_vie_gradient).  Returns (J_obj, d_eps,
-    d_sigma, J)."""
+    per-voxel sensitivities (marie_vie_gradient).  ``solve_op`` (default
+    ``op``) runs the two GMRES solves: a handle on the same body and
+    materials, e.g. one with the float-float complex128 N operator while
+    ``op`` holds native complex128 with K.  Returns (J_obj, d_eps, d_sigma,
+    J)."""
     import torch
+    sop = op if solve_op is None else solve_op
     if J is None:
-        J, _rep = op.gmres(b, tol=tol, mode=mode)
+        J, _rep = sop.gmres(b, tol=tol, mode=mode)
     Jobj, M, P, E, H, b1 = b1_objective(op, J, Ue, Ub, roi)
     Ns, l = op.Ns, 4 if op.pwl else 1
     r = torch.as_tensor(np.asarray(roi), device="cuda")
@@ -269,7 +273,7 @@ def b1_objective_gradient(op: VieOperator, b, Ue, Ub, roi, *, tol=1e-6, mode="mi
     mu0 = 4e-7 * np.pi
     gM = op.apply_hfield_adjoint(w) * (mu0 / len(roi))
     g = op.gradient_source(J, gM, M, P)
-    lam, _repa = op.gmres(g, tol=tol, mode=mode, adjoint=True)
+    lam, _repa = sop.gmres(g, tol=tol, mode=mode, adjoint=True)
     de, ds = op.gradient(J, lam, E, M, P)
     return Jobj, de, ds, J
 

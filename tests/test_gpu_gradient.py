@@ -6,9 +6,7 @@ with respect to each body voxel's eps_r and sigma (GPU).
   of the objective recomputed with perturbed materials, complex128 solves
   to 1e-12, on 32 seeded voxels and both material parameters; per-voxel
   relative agreement within 1e-5 (measured 1e-9 to 1e-6).
-* 96^3 PWL ellipsoid with a 20^3 ROI (the adjoint-gradient configuration's
-  size): the gradient from mixed-precision solves against the one from
-  complex128 solves, within 1e-3.
+* The configuration's full size (96^3) is checked in test_gpu_gradient96.py.
 * torch.autograd through vie.b1_objective_autograd: backward returns the
   adjoint sensitivities, chained through a function of the materials.
 """
@@ -76,36 +74,6 @@ def test_b1_gradient_matches_finite_differences():
             adj = de[s] if which == "er" else ds[s]
             scale = scale_e if which == "er" else scale_s
             assert fd != 0 and abs(fd - adj) <= 1e-5 * abs(fd) + 1e-9 * scale, (which, s, fd, adj, scale)
-
-
-@pytest.mark.gpu
-def test_b1_gradient_mixed_matches_fp64_at_96():
-    from marie_gb300 import assemble_green, phantoms
-    from marie_gb300 import vie
-    res, freq, pwl = 2e-3, 297.2e6, True
-    body = phantoms.ellipsoid_phantom(96, res, seed=0)
-    ivN = assemble_green(body.n, res, freq, pwl, "N")
-    ivK = assemble_green(body.n, res, freq, pwl, "K")
-    op = _setup(body, res, freq, pwl, 3, ivN, ivK)
-    del ivN, ivK
-    loops, radius = phantoms.loop_outside((0.080, 0.065, 0.090), gap=0.01, radius=0.05)
-    Ue = op.incident_loops(body.origin, loops, radius, nseg=64)
-    Ub = torch.zeros_like(Ue)
-    # seeded 20^3 ROI inside the body
-    rng = np.random.default_rng(5)
-    ijk = np.stack(np.unravel_index(body.idxS, body.n, order="F"), 1)
-    c0 = ijk[rng.integers(body.idxS.size)]
-    lo = np.clip(c0 - 10, 0, np.array(body.n) - 20)
-    roi = np.nonzero(np.all((ijk >= lo) & (ijk < lo + 20), axis=1))[0]
-    assert roi.size > 1000
-    b = _rhs(op, body, freq, pwl, Ue)
-    Jm, dem, dsm, _ = vie.b1_objective_gradient(op, b, Ue, Ub, roi, tol=1e-6, mode="mixed")
-    Jf, def_, dsf, _ = vie.b1_objective_gradient(op, b, Ue, Ub, roi, tol=1e-9, mode="fp64")
-    assert abs(Jm - Jf) <= 1e-4 * abs(Jf)
-    for a, ref in ((dem, def_), (dsm, dsf)):
-        a, ref = a.cpu().numpy(), ref.cpu().numpy()
-        assert np.linalg.norm(a - ref) <= 1e-3 * np.linalg.norm(ref)
-    op.close()
 
 
 @pytest.mark.gpu
