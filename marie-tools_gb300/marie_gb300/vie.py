@@ -183,11 +183,11 @@ def ie_solver_vie(fN: VieOperator, Ue, ce, Mr, Mc, idxS, tol, restart=50, maxit=
     chi = np.tile((1.0 / mr) * mc, ql)
     U = _to_cuda(Ue, torch.complex128).reshape(fN.Nb, -1)
     rhs = ce * _to_cuda(chi, torch.complex128)[:, None] * U
-    Jb, _it, _rv = is_gmres_vie(fN, rhs, restart, tol, maxit, None, mode=mode)
+    Jd, _it, _rv = is_gmres_vie(fN, rhs, restart, tol, maxit, None, mode=mode)
+    Jd = Jd.reshape(fN.Nb, -1)
+    Jb = Jd if isinstance(Ue, torch.Tensor) else Jd.cpu().numpy()     # Jb follows Ue
     if X is None:
         return Jb, [], [], []
-    Jd = Jb if isinstance(Jb, torch.Tensor) else _to_cuda(Jb, torch.complex128)
-    Jd = Jd.reshape(fN.Nb, -1)
     UJ = (U.t() @ Jd).cpu().numpy()                # Ue.' * Jb: N_ports x N_ports
     Xn = np.asarray(X, dtype=np.complex128)
     Z = Xn.T @ (UJ @ Xn)

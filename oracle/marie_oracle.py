@@ -567,6 +567,36 @@ def block_spectrum_dense(IV: np.ndarray, key, kernel: str = "N", workers=None) -
     return _fftn(E, workers=workers)
 
 
+def _mac(acc, a, b, sgn):
+    """acc += sgn * a * b elementwise, split over the host cores (numpy
+    releases the interpreter lock inside its loops)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    fa, fb, fo = a.reshape(-1), b.reshape(-1), acc.reshape(-1)
+    n = fo.size
+    k = max(1, min(os.cpu_count() or 1, n // (1 << 18)))
+    step = (n + k - 1) // k
+
+    def work(lo):
+        hi = min(n, lo + step)
+        t = fa[lo:hi] * fb[lo:hi]
+        if sgn > 0:
+            fo[lo:hi] += t
+        else:
+            fo[lo:hi] -= t
+
+    if k == 1:
+        work(0)
+        return
+    global _POOL
+    if _POOL is None:
+        _POOL = ThreadPoolExecutor(max_workers=os.cpu_count() or 1)
+    list(_POOL.map(work, range(0, n, step)))
+
+
+_POOL = None
+
+
 def mvp_op_dense(Jin: np.ndarray, IV: np.ndarray, op: str = "N", adjoint: bool = False,
                  spectra: dict | None = None, workers=None) -> np.ndarray:
     """mvp_{N,K}{,_herm_adj}_{pwc,pwl}_tucker.m (the block products of
@@ -597,10 +627,7 @@ def mvp_op_dense(Jin: np.ndarray, IV: np.ndarray, op: str = "N", adjoint: bool =
                 spectra[key] = blk
         bc = blk.conj() if adjoint else blk
         for p, q, sg, _cj in lst:
-            if sg > 0:
-                acc[p] += bc * fJ[q]
-            else:
-                acc[p] -= bc * fJ[q]
+            _mac(acc[p], bc, fJ[q], sg)
         del blk, bc
     Jout = np.empty(Jin.shape, dtype=complex)
     for p in range(C):

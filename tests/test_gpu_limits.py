@@ -73,7 +73,7 @@ def test_create_refuses_grid_beyond_shared_memory():
 @pytest.mark.gpu
 def test_memory_cap_gives_oom():
     from marie_gb300 import _lib
-    P = Problem((8, 8, 8), False, seed=2, iv_scale=0.2)
+    P = Problem((8, 8, 8), False, seed=2, iv_scale=0.02)
     with pytest.raises(_lib.MarieError) as ei:
         P.gpu_operator(precisions=1, max_rhs=1, mem_cap_bytes=1024)
     assert ei.value.status == 2 and "cap" in str(ei.value)
