@@ -331,6 +331,10 @@ marie_status marie_svie_pfft_destroy(marie_svie_pfft* h);
  * ms[3] y-inverse, ms[4] x-inverse + epilogue.  ms[5] = whole application. */
 marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,
                                double* ms, void* stream);
+/* Shape of a handle: out[0..2] = the caller's grid edges n1, n2, n3,
+ * out[3] = ql (3 PWC, 12 PWL), out[4] = N_s body voxels, out[5] = N_b body
+ * unknowns (dims.N_b of geo_assembly.m). */
+marie_status marie_vie_info(marie_vie* h, int64_t* out);
 /* Workspace right-hand sides per matvec chunk and the z-pass tile width:
  * out[0] = chunk, out[1] = tile width (pencils x interleaved right-hand
  * sides), out[2..3] reserved (0). */

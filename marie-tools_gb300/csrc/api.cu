@@ -747,6 +747,17 @@ marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
   return MARIE_OK;
 }
 
+marie_status marie_vie_info(marie_vie* h, int64_t* out) {
+  if (!h || !out) { set_error("info: NULL argument"); return MARIE_ERR_BAD_ARG; }
+  out[0] = h->on1 ? h->on1 : h->n1;
+  out[1] = h->on1 ? h->on2 : h->n2;
+  out[2] = h->on1 ? h->on3 : h->n3;
+  out[3] = h->C;
+  out[4] = h->Ns;
+  out[5] = h->Nb;
+  return MARIE_OK;
+}
+
 marie_status marie_vie_set_materials(marie_vie* h, const double* Mr_body) {
   if (!h || !Mr_body) { set_error("set_materials: NULL argument"); return MARIE_ERR_BAD_ARG; }
   std::vector<std::complex<double>> mr(h->Ns);

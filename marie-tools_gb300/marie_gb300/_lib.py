@@ -103,6 +103,7 @@ _PROTOS = {
     "marie_vie_tiles": (ct.c_int, [_vp, ct.c_int32, c_int32_p]),
     "marie_vie_release_workspace": (ct.c_int, [_vp]),
     "marie_vie_set_materials": (ct.c_int, [_vp, c_double_p]),
+    "marie_vie_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64)]),
     "marie_vie_fields": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, _vp, _vp, _vp, ct.c_int32, _vp]),
     "marie_vie_absorbed_power": (ct.c_int, [_vp, _vp, ct.c_int32, c_double_p, _vp]),
     "marie_vie_b1_plus": (ct.c_int, [_vp, _vp, ct.c_int32, _vp, _vp]),

@@ -16,6 +16,14 @@
  *   [x, iter, resvec] = marie_mex('gmres', h, b, restart, tol, maxit, x0 [, mode])
  *                                                   % is_gmres_vie.m:1; b may be N_b x nrhs
  *   marie_mex('destroy', h)
+ *   hp = marie_mex('svie_pfft_create', h, N_sie, pfft_PS, pfft_Z_cc, pfft_Z_bc_N, ext_Mc_inv [, M1, M2])
+ *       h: handle on the pFFT grid (MREDM.operators.pfft_N); sparse complex operands as in
+ *       ie_solver_svie_pfft.m:19-26
+ *   Vout = marie_mex('svie_pfft', hp, Jcb)           % mvp_svie_pfft.m:1 (operands bound in hp)
+ *   marie_mex('svie_pfft_destroy', hp)
+ *   Ue = marie_mex('incident_wire', h, 'E' | 'H', origin, rp, rn, r2 [, Jw])
+ *       wire bases as columns rp / rn / r2 (3 x N_tri, wvie_mrgf_assembly.m:20-22), Jw N_tri x nports
+ *       (default: ones); returns invG of the tested field on the body, N_b x nports
  *   I_V = marie_mex('assemble', [n1 n2 n3], PWX, res, freq, 'N' | 'K' [, 'exact' | 'standin'])
  *       assembly_N.m / assembly_K.m on the GPU, (n1, n2, n3, pwx, 6 | 3) complex; near zone 'exact'
  *       (default: the same integrals as the reference's DIRECTFN surface-surface near zone) or the
@@ -243,6 +251,99 @@ static void cmd_assemble(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prh
                                 (double*)mxGetComplexDoubles(plhs[0])));
 }
 
+/* MATLAB sparse (compressed columns, 1 column pointer per column) -> CSR
+ * with 0-based indices; arrays allocated with mxCalloc. */
+static marie_csr sparse_to_csr(const mxArray* A, const char* what) {
+  if (!mxIsSparse(A) || !mxIsDouble(A)) mexErrMsgIdAndTxt("marie:BAD_ARG", "%s must be a sparse double matrix", what);
+  const mwSize m = mxGetM(A), n = mxGetN(A);
+  const mwIndex* jc = mxGetJc(A);
+  const mwIndex* ir = mxGetIr(A);
+  const mwIndex nnz = jc[n];
+  const int cplx = mxIsComplex(A);
+  const double* re = cplx ? NULL : mxGetDoubles(A);
+  const mxComplexDouble* cz = cplx ? mxGetComplexDoubles(A) : NULL;
+  int64_t* rp = (int64_t*)mxCalloc(m + 1, sizeof(int64_t));
+  int64_t* ci = (int64_t*)mxCalloc(nnz > 0 ? nnz : 1, sizeof(int64_t));
+  double* v = (double*)mxCalloc(2 * (nnz > 0 ? nnz : 1), sizeof(double));
+  for (mwIndex k = 0; k < nnz; ++k) rp[ir[k] + 1]++;
+  for (mwSize r = 0; r < m; ++r) rp[r + 1] += rp[r];
+  int64_t* next = (int64_t*)mxCalloc(m > 0 ? m : 1, sizeof(int64_t));
+  for (mwSize r = 0; r < m; ++r) next[r] = rp[r];
+  for (mwSize c = 0; c < n; ++c)
+    for (mwIndex k = jc[c]; k < jc[c + 1]; ++k) {
+      const int64_t d = next[ir[k]]++;
+      ci[d] = (int64_t)c;
+      v[2 * d] = cplx ? cz[k].real : re[k];
+      v[2 * d + 1] = cplx ? cz[k].imag : 0.0;
+    }
+  marie_csr out;
+  out.rows = (int64_t)m;
+  out.cols = (int64_t)n;
+  out.nnz = (int64_t)nnz;
+  out.row_ptr = rp;
+  out.col_idx = ci;
+  out.val = v;
+  return out;
+}
+
+static void cmd_svie_pfft_create(mxArray** plhs, int nrhs, const mxArray** prhs) {
+  if (nrhs < 7) mexErrMsgIdAndTxt("marie:BAD_ARG", "svie_pfft_create: expected h, N_sie, PS, Z_cc, Z_bc_N, ext_Mc_inv");
+  marie_svie_pfft_desc d;
+  memset(&d, 0, sizeof(d));
+  d.grid_op = get_handle(prhs[1]);
+  d.n_sie = (int64_t)scalar(prhs[2], "N_sie");
+  d.PS = sparse_to_csr(prhs[3], "pfft_PS");
+  d.n_b = d.PS.cols - d.n_sie;
+  d.Z_cc = sparse_to_csr(prhs[4], "pfft_Z_cc");
+  d.Z_bc_N = sparse_to_csr(prhs[5], "pfft_Z_bc_N");
+  if (!mxIsComplex(prhs[6]) || !mxIsDouble(prhs[6])) mexErrMsgIdAndTxt("marie:BAD_ARG", "ext_Mc_inv must be complex double");
+  d.ext_Mc_inv = (const double*)mxGetComplexDoubles(prhs[6]);
+  if (nrhs > 7 && !mxIsEmpty(prhs[7])) d.M1 = mxGetDoubles(prhs[7]);
+  if (nrhs > 8 && !mxIsEmpty(prhs[8])) d.M2 = mxGetDoubles(prhs[8]);
+  marie_svie_pfft* hp = NULL;
+  check(marie_svie_pfft_create(&hp, &d));
+  plhs[0] = mxCreateNumericMatrix(1, 1, mxUINT64_CLASS, mxREAL);
+  *(uint64_t*)mxGetData(plhs[0]) = (uint64_t)(uintptr_t)hp;
+}
+
+static marie_status svie_pfft_apply_as_vie(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs,
+                                           void* stream) {
+  return marie_svie_pfft_apply((marie_svie_pfft*)(void*)h, prec, x, y, nrhs, stream);
+}
+
+/* Ue = marie_mex('incident_wire', h, 'E'|'H', origin, rp, rn, r2 [, Jw]) */
+static void cmd_incident_wire(mxArray** plhs, int nrhs, const mxArray** prhs, marie_vie* h) {
+  if (nrhs < 7) mexErrMsgIdAndTxt("marie:BAD_ARG", "incident_wire: expected h, 'E'|'H', origin, rp, rn, r2");
+  char kind[4] = {0};
+  if (!mxIsChar(prhs[2]) || mxGetString(prhs[2], kind, sizeof(kind)) || (strcmp(kind, "E") && strcmp(kind, "H")))
+    mexErrMsgIdAndTxt("marie:BAD_ARG", "field must be 'E' or 'H'");
+  const double* org = mxGetDoubles(prhs[3]);
+  if (!org || mxGetNumberOfElements(prhs[3]) != 3) mexErrMsgIdAndTxt("marie:BAD_ARG", "origin must be 3 doubles");
+  const int32_t ntri = (int32_t)mxGetN(prhs[4]);
+  for (int i = 4; i < 7; ++i)
+    if (!mxIsDouble(prhs[i]) || mxGetM(prhs[i]) != 3 || (int32_t)mxGetN(prhs[i]) != ntri)
+      mexErrMsgIdAndTxt("marie:BAD_ARG", "rp, rn, r2 must be 3 x N_tri doubles");
+  const double* cf = NULL;
+  int32_t nports = 1;
+  if (nrhs > 7 && !mxIsEmpty(prhs[7])) {
+    const mxArray* J = prhs[7];
+    if (!mxIsComplex(J) || (int32_t)mxGetM(J) != ntri) mexErrMsgIdAndTxt("marie:BAD_ARG", "Jw must be complex N_tri x nports");
+    nports = (int32_t)mxGetN(J);
+    cf = (const double*)mxGetComplexDoubles(J);     /* column p = port p: nports x N_tri row-major */
+  }
+  int64_t info[6];
+  check(marie_vie_info(h, info));
+  const int64_t Nb = info[5];
+  void* d = NULL;
+  if (cudaMalloc(&d, (size_t)Nb * nports * 16)) mexErrMsgIdAndTxt("marie:OOM", "device allocation failed");
+  marie_status st = marie_incident_wire(h, kind[0] == 'E' ? 0 : 1, org, mxGetDoubles(prhs[4]), mxGetDoubles(prhs[5]),
+                                        mxGetDoubles(prhs[6]), ntri, cf, nports, 4, 2, d, NULL);
+  plhs[0] = mxCreateNumericMatrix((mwSize)Nb, (mwSize)nports, mxDOUBLE_CLASS, mxCOMPLEX);
+  if (st == MARIE_OK) cudaMemcpy(mxGetComplexDoubles(plhs[0]), d, (size_t)Nb * nports * 16, D2H);
+  cudaFree(d);
+  check(st);
+}
+
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs < 1 || !mxIsChar(prhs[0])) mexErrMsgIdAndTxt("marie:BAD_ARG", "first argument must be a command string");
   char cmd[32];
@@ -252,6 +353,9 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs < 2) mexErrMsgIdAndTxt("marie:BAD_ARG", "missing handle");
   marie_vie* h = get_handle(prhs[1]);
   if (!strcmp(cmd, "destroy")) { check(marie_vie_destroy(h)); return; }
+  if (!strcmp(cmd, "svie_pfft_create")) { cmd_svie_pfft_create(plhs, nrhs, prhs); return; }
+  if (!strcmp(cmd, "svie_pfft_destroy")) { check(marie_svie_pfft_destroy((marie_svie_pfft*)(void*)h)); return; }
+  if (!strcmp(cmd, "incident_wire")) { cmd_incident_wire(plhs, nrhs, prhs, h); return; }
   /* lengths: body vector N_b is taken from the input length per rhs via the handle's apply checks */
   if (nrhs < 3) mexErrMsgIdAndTxt("marie:BAD_ARG", "missing input array");
   const mwSize* d = mxGetDimensions(prhs[2]);
@@ -259,6 +363,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (!strcmp(cmd, "mvp_vie")) { cmd_apply(marie_vie_apply, rows, plhs, prhs[2], h); return; }
   if (!strcmp(cmd, "mvp_vie_adj")) { cmd_apply(marie_vie_apply_adjoint, rows, plhs, prhs[2], h); return; }
   if (!strcmp(cmd, "gmres")) { cmd_gmres(nlhs, plhs, nrhs, prhs, h, rows); return; }
+  if (!strcmp(cmd, "svie_pfft")) { cmd_apply(svie_pfft_apply_as_vie, rows, plhs, prhs[2], h); return; }
   /* grid operators: Jin is n1 x n2 x n3 x C */
   const int64_t grid = (int64_t)mxGetNumberOfElements(prhs[2]);
   if (!strcmp(cmd, "mvp_N")) { cmd_apply(marie_vie_apply_N, grid, plhs, prhs[2], h); return; }

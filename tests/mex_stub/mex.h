@@ -18,6 +18,10 @@ bool mxIsComplex(const mxArray*);
 bool mxIsStruct(const mxArray*);
 bool mxIsChar(const mxArray*);
 bool mxIsEmpty(const mxArray*);
+bool mxIsSparse(const mxArray*);
+size_t mxGetN(const mxArray*);
+mwIndex* mxGetIr(const mxArray*);
+mwIndex* mxGetJc(const mxArray*);
 size_t mxGetNumberOfElements(const mxArray*);
 size_t mxGetM(const mxArray*);
 void* mxGetData(const mxArray*);
