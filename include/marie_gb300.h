@@ -74,7 +74,11 @@ typedef struct {
   /* K operator (optional): Tucker (3 PWC / 30 PWL, index j*3+k) or dense (n1,n2,n3,pwx,3). */
   const marie_tucker_block* tucker_K;
   const double* dense_K;
-  int32_t precisions;        /* bit mask: 1 = build C128 path, 2 = build C64 path */
+  int32_t precisions;        /* bit mask: 1 = build the native C128 path, 2 = the C64 path, 4 = C128 in
+                                float-float arithmetic (edges 16*NB; exclusive with 1), 8 = keep the
+                                Tucker factors of tucker_N and re-expand the C64 spectrum at the start of
+                                every C64 application of N / N^H, as mvp_N_pwl_tucker.m:31 re-expands
+                                its blocks in every product (needs bit 2, tucker_N, edges 16*NB) */
   int32_t max_rhs;           /* largest nrhs per apply/solve call (workspace sizing) */
   int64_t mem_cap_bytes;     /* 0 = no cap; otherwise create/solve fail with OOM above it */
 } marie_vie_desc;

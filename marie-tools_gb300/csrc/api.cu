@@ -410,6 +410,11 @@ static marie_status launch_matvec_ev(marie_vie* h, int mode, int op, const cplx<
   a.out_rs = out_rs;
   const int n1 = h->n1, n2 = h->n2, n3 = h->n3, C = h->C;
   const size_t sz = sizeof(cplx<T>);
+  if constexpr (std::is_same<T, float>::value) {
+    // the reference's form: the Tucker blocks re-expanded for this application
+    if (h->tkf.active && (op == OP_N || op == OP_N_ADJ) && !env_int("MARIE_GENERIC_FFT", 0))
+      MARIE_TRY(tucker_expand_c64(h, stream));
+  }
   for (int r0 = 0; r0 < nrhs; r0 += ps.ws_rhs) {
     const int nr = std::min(ps.ws_rhs, nrhs - r0);
     const bool fast = four_step_edge(n1) && four_step_edge(n2) && four_step_edge(n3) &&
@@ -539,7 +544,14 @@ static marie_status validate_desc(const marie_vie_desc* d, std::vector<int64_t>&
   if (!d->idx_solution || d->n_b <= 0) { set_error("idx_solution is empty"); return MARIE_ERR_BAD_ARG; }
   if (!d->Mr) { set_error("Mr is NULL"); return MARIE_ERR_BAD_ARG; }
   if (!d->tucker_N && !d->dense_N) { set_error("neither tucker_N nor dense_N given"); return MARIE_ERR_BAD_ARG; }
-  if (d->precisions < 1 || d->precisions > 7) { set_error("precisions must be a nonzero mask of bits 1, 2 and 4"); return MARIE_ERR_BAD_ARG; }
+  if (d->precisions < 1 || d->precisions > 15 || !(d->precisions & 7)) {
+    set_error("precisions must be a mask of bits 1, 2, 4 (at least one) and 8");
+    return MARIE_ERR_BAD_ARG;
+  }
+  if ((d->precisions & 8) && (!d->tucker_N || !(d->precisions & 2))) {
+    set_error("precisions bit 8 (per-application Tucker expansion) needs tucker_N and the complex64 state (bit 2)");
+    return MARIE_ERR_BAD_ARG;
+  }
   if ((d->precisions & 1) && (d->precisions & 4)) {
     set_error("precisions bits 1 (native complex128) and 4 (float-float complex128) are exclusive");
     return MARIE_ERR_BAD_ARG;
@@ -707,6 +719,13 @@ static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
     }
   }
   if ((st = build_spectra(h, d)) != MARIE_OK) return fail(st);
+  if (d->precisions & 8) {
+    if (!four_step_grid(h)) {
+      set_error("precisions bit 8 needs a grid with edges 16*NB, NB <= 8 (the four-step complex64 path)");
+      return fail(MARIE_ERR_BAD_ARG);
+    }
+    if ((st = tucker_keep_c64(h, d->tucker_N)) != MARIE_OK) return fail(st);
+  }
   if (h->precisions & 1) h->p64.built = true;
   if (h->precisions & 2) h->p32.built = true;
   if (h->precisions & 4) h->pff.built = true;

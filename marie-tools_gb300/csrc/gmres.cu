@@ -231,6 +231,7 @@ struct GmState {
   double* resid;  // [nrhs]   |g_{k+1}|
   double* tolabs; // [nrhs]
   int* kr;        // [nrhs]   Arnoldi steps in the current cycle
+  double* hist;   // [nrhs][m] |g_{k+1}| after step k of the current cycle
   unsigned char* incyc;  // [nrhs] in the Arnoldi loop of the current cycle
   zd* part;       // [nrhs][m+1][nch]
   double* npart;  // [nrhs][nch]
@@ -281,6 +282,7 @@ __global__ void k_givens(GmState st, int k, int m, int nrhs) {
   g[k] = zd{c * gk.x, c * gk.y};
   const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
   st.resid[r] = res;
+  st.hist[(int64_t)r * m + k] = res;
   st.kr[r] = k + 1;
   if (!isfinite(res) || !isfinite(hk1)) {
     st.incyc[r] = 0;
@@ -495,8 +497,10 @@ __global__ void k_bytes(const unsigned char* __restrict__ src, unsigned char* __
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
 }
 
+// Behind the slots: a region of kMaxRestart doubles per rhs for the residual
+// history of the Arnoldi steps between two host synchronisations.
 static marie_status chan_reserve(marie_vie* h, int nrhs) {
-  const size_t need = (size_t)kSlots * 16 * std::max(nrhs, 1);
+  const size_t need = (size_t)(kSlots * 16 + kMaxRestart * 8) * std::max(nrhs, 1);
   if (h->hio_cap >= need) return MARIE_OK;
   if (h->hio) cudaFreeHost(h->hio);
   h->hio = nullptr;
@@ -537,6 +541,27 @@ static marie_status chan_get(marie_vie* h, int slot, int nrhs, const void* src, 
 }
 static void chan_take(marie_vie* h, int slot, int nrhs, void* dst, size_t bytes) {
   memcpy(dst, chan_slot(h, slot, nrhs), bytes);
+}
+static unsigned char* chan_hist(marie_vie* h, int nrhs) { return chan_slot(h, kSlots, nrhs); }
+static marie_status chan_get_hist(marie_vie* h, int nrhs, const double* src, size_t bytes, cudaStream_t s) {
+  MARIE_TRY(chan_reserve(h, nrhs));
+  unsigned char* qd = nullptr;
+  MARIE_CUDA_TRY(cudaHostGetDevicePointer((void**)&qd, chan_hist(h, nrhs), 0));
+  k_bytes<<<8, 256, 0, s>>>((const unsigned char*)src, qd, (int)bytes);
+  MARIE_LAUNCH_CHECK();
+  return MARIE_OK;
+}
+
+// Arnoldi steps between host synchronisations (MARIE_SYNC_STEPS, default 8):
+// the device masks stop the work of right-hand sides that leave the cycle,
+// the host reads their residual history at each synchronisation.
+static int sync_steps() {
+  static const int v = [] {
+    const char* e = getenv("MARIE_SYNC_STEPS");
+    const int n = e ? atoi(e) : 0;
+    return n >= 1 ? n : 8;
+  }();
+  return v;
 }
 
 static dim3 vgrid(int64_t Nb, int nrhs) {
@@ -580,6 +605,7 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
   MARIE_TRY(sc.get(&st.resid, nrhs));
   MARIE_TRY(sc.get(&st.tolabs, nrhs));
   MARIE_TRY(sc.get(&st.kr, nrhs));
+  MARIE_TRY(sc.get(&st.hist, (size_t)nrhs * m));
   MARIE_TRY(sc.get(&st.incyc, nrhs));
   MARIE_TRY(sc.get(&st.part, (size_t)nrhs * mp1 * nch));
   MARIE_TRY(sc.get(&st.npart, (size_t)nrhs * nch));
@@ -614,7 +640,6 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     if (rel > tolrel[r] && maxit > 0) { start[r] = 1; ++nstart; }
   }
   std::vector<unsigned char> incyc(nrhs), prev(nrhs);
-  std::vector<double> resid(nrhs);
   std::vector<int> kr(nrhs);
   int outit = 0;
   while (nstart > 0) {
@@ -626,6 +651,7 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     MARIE_LAUNCH_CHECK();
     for (int r = 0; r < nrhs; ++r) if (start[r]) log[r].outer = outit;
     incyc = start;
+    int k_win = 0;     // first step not yet logged
     for (int k = 0; k < m; ++k) {
       MARIE_TRY(launch_matvec<T>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N,
                                  V + (int64_t)k * ld, vrs, V + (int64_t)(k + 1) * ld, vrs, nrhs, st.incyc, s));
@@ -643,19 +669,26 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
       MARIE_LAUNCH_CHECK();
       k_givens<<<sb, 128, 0, s>>>(st, k, m, nrhs);
       MARIE_LAUNCH_CHECK();
+      if ((k + 1) % sync_steps() != 0 && k + 1 < m) continue;
       prev = incyc;
       MARIE_TRY(chan_get(h, SLOT_INCYC, nrhs, st.incyc, nrhs, s));
-      MARIE_TRY(chan_get(h, SLOT_RESID, nrhs, st.resid, nrhs * sizeof(double), s));
+      MARIE_TRY(chan_get(h, SLOT_KR, nrhs, st.kr, nrhs * sizeof(int), s));
+      MARIE_TRY(chan_get_hist(h, nrhs, st.hist, (size_t)nrhs * m * sizeof(double), s));
       MARIE_CUDA_TRY(cudaStreamSynchronize(s));
       chan_take(h, SLOT_INCYC, nrhs, incyc.data(), nrhs);
-      chan_take(h, SLOT_RESID, nrhs, resid.data(), nrhs * sizeof(double));
+      chan_take(h, SLOT_KR, nrhs, kr.data(), nrhs * sizeof(int));
+      const double* hist = reinterpret_cast<const double*>(chan_hist(h, nrhs));
       int any = 0;
       for (int r = 0; r < nrhs; ++r) {
         if (!prev[r]) continue;
-        log[r].resvec.push_back(resid[r] / bnorm[r]);
-        log[r].iters++;
+        // steps [k_win, kr) of this window ran for r
+        for (int j = k_win; j < kr[r]; ++j) {
+          log[r].resvec.push_back(hist[(size_t)r * m + j] / bnorm[r]);
+          log[r].iters++;
+        }
         if (incyc[r]) any = 1;
       }
+      k_win = k + 1;
       if (!any) break;
     }
     // finalize the cycle of every rhs that ran it

@@ -63,6 +63,22 @@ struct PrecState {
   int TY = 1, TXY = 1, TX = 1;
 };
 
+// Tucker factors kept on the device (FP32) for the per-application
+// expansion of the complex64 spectrum (tucker.cu, precisions bit 8).
+struct TuckerDev {
+  struct Block {
+    int r1 = 0, r2 = 0, r3 = 0;
+    cplx<float>* G = nullptr;    // r1 r2 r3, then U1 (r1 x 2n1), U2, U3 in the same allocation
+    cplx<float>* U1 = nullptr;
+    cplx<float>* U2 = nullptr;
+    cplx<float>* U3 = nullptr;
+  };
+  bool active = false;
+  std::vector<Block> blocks;
+  cplx<float>* P1 = nullptr;     // work: r1 r2 x 2n3
+  cplx<float>* P2 = nullptr;     // work: r1 x 2n2 x 2n3
+};
+
 }  // namespace marie
 
 struct marie_vie {
@@ -91,6 +107,7 @@ struct marie_vie {
   marie::PrecState<double> p64;
   marie::PrecState<float> p32;
   marie::PrecState<marie::ff> pff;   // complex128 I/O, float-float arithmetic (precisions bit 4)
+  marie::TuckerDev tkf;              // precisions bit 8: complex64 spectrum re-expanded per application
   std::vector<void*> allocs;
   // GMRES workspace pool: the buffers a solve requests, in request order,
   // kept across solves and grown on demand (marie_vie_release_workspace
@@ -135,6 +152,11 @@ template <typename T>
 marie_status launch_fast_chunk(marie_vie* h, int op, MvArgs<T>& a, int nb, cudaStream_t stream, cudaEvent_t* ev);
 
 marie_status build_spectra(marie_vie* h, const marie_vie_desc* d);
+
+// Per-application Tucker expansion (tucker.cu): keep the N operator's
+// factors at create; rebuild the complex64 full spectrum on `s`.
+marie_status tucker_keep_c64(marie_vie* h, const marie_tucker_block* tk);
+marie_status tucker_expand_c64(marie_vie* h, cudaStream_t s);
 
 // n-point Gauss-Legendre rule on [-1, 1], nodes ascending (host).
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);

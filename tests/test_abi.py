@@ -64,6 +64,9 @@ def test_rejects_bad_descriptors(lib):
         dict(base, freq=0.0),
         dict(base, precisions=0),
         dict(base, precisions=8),
+        dict(base, precisions=16),
+        dict(base, precisions=2 | 8),            # per-application Tucker expansion without Tucker blocks
+        dict(base, precisions=1 | 8),            # ... or without the complex64 state
         dict(base, precisions=5),                # native and float-float complex128 together
         dict(base, max_rhs=0),
         dict(base, n_b=16),                      # not a multiple of 3
