@@ -339,6 +339,16 @@ marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* 
  * out[3] = ql (3 PWC, 12 PWL), out[4] = N_s body voxels, out[5] = N_b body
  * unknowns (dims.N_b of geo_assembly.m). */
 marie_status marie_vie_info(marie_vie* h, int64_t* out);
+/* Autotuner of the FFT tiles: times `reps` applications of mvp_vie in
+ * precision prec on x (device, nrhs x N_b; y receives the results) for every
+ * z-pass tile width (a power of two <= 16: pencils x interleaved right-hand
+ * sides) whose shared memory fits one CTA and whose bundles fit the handle's
+ * work arrays, and keeps the fastest for later calls.  widths / ms (host,
+ * cap entries) receive the widths tried and their mean times; *count the
+ * number tried.  No counterpart in the reference (MATLAB's fftn plans its
+ * own transforms). */
+marie_status marie_vie_autotune(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,
+                                int32_t* widths, double* ms, int32_t cap, int32_t* count, void* stream);
 /* Workspace right-hand sides per matvec chunk and the z-pass tile width:
  * out[0] = chunk, out[1] = tile width (pencils x interleaved right-hand
  * sides), out[2..3] reserved (0). */

@@ -307,6 +307,7 @@ static marie_status alloc_workspace(marie_vie* h, PrecState<T>& ps) {
   if (ws > Wz) ws = (ws + Wz - 1) / Wz * Wz;   // whole bundles
   ps.ws_rhs = ws;
   const int64_t alloc = (int64_t)(ws + Wz - 1) / Wz * Wz;   // any chunk of <= ws rhs fits whole bundles
+  ps.ws_cap = (int)alloc;
   MARIE_TRY(dev_alloc(h, (void**)&ps.T1, (size_t)alloc * per * sizeof(cplx<T>)));
   MARIE_TRY(dev_alloc(h, (void**)&ps.S, (size_t)alloc * per * 2 * sizeof(cplx<T>)));
   return MARIE_OK;
@@ -737,6 +738,58 @@ static marie_status create_grid(marie_vie** out, const marie_vie_desc* d) {
   return MARIE_OK;
 }
 
+// Autotuner of the z-pass tile width: time `reps` applications of mvp_vie
+// on x (nrhs right-hand sides) for every power-of-two width whose shared
+// memory fits a CTA and whose bundles fit the work arrays, keep the fastest.
+template <typename T>
+static marie_status autotune_state(marie_vie* h, PrecState<T>& ps, const void* x, void* y, int nrhs, int reps,
+                                   cudaStream_t s, int32_t* widths, double* ms, int32_t cap, int32_t* count) {
+  const int C = h->C;
+  const size_t sz = sizeof(cplx<T>);
+  const bool fast = four_step_grid(h) && !env_int("MARIE_GENERIC_FFT", 0);
+  const int keep = ps.TX;
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  int best = keep, n = 0;
+  double best_ms = 1e300;
+  marie_status st = MARIE_OK;
+  for (int W = 1; W <= 16 && st == MARIE_OK; W *= 2) {
+    if ((ps.ws_rhs + W - 1) / W * W > ps.ws_cap) continue;
+    if (fast) {
+      if (kz4_smem<T>(h->n3, C, W) > kSmemOptin) continue;
+    } else {
+      const GenericSmem g = generic_smem(h->n1, h->n2, h->n3, C, sz, 1, 1, 1, W);
+      if (g.x > kSmemOptin || g.y > kSmemOptin || g.z > kSmemOptin) continue;
+    }
+    ps.TX = W;
+    float total = 0;
+    for (int r = 0; r <= reps && st == MARIE_OK; ++r) {     // r = 0: warm-up
+      cudaEventRecord(t0, s);
+      st = launch_matvec_ev<T>(h, MV_VIE, OP_N, (const cplx<typename IoOf<T>::type>*)x, h->Nb,
+                               (cplx<typename IoOf<T>::type>*)y, h->Nb, nrhs, nullptr, s, nullptr);
+      cudaEventRecord(t1, s);
+      if (cudaEventSynchronize(t1) != cudaSuccess) { set_error("autotune: device error"); st = MARIE_ERR_CUDA; }
+      float v = 0;
+      cudaEventElapsedTime(&v, t0, t1);
+      if (r > 0) total += v;
+    }
+    if (st != MARIE_OK) break;
+    const double avg = total / reps;
+    if (n < cap) {
+      widths[n] = W;
+      ms[n] = avg;
+    }
+    ++n;
+    if (avg < best_ms) { best_ms = avg; best = W; }
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  ps.TX = st == MARIE_OK ? best : keep;
+  *count = n;
+  return st;
+}
+
 extern "C" {
 
 marie_status marie_vie_create(marie_vie** out, const marie_vie_desc* d) {
@@ -891,6 +944,23 @@ marie_status marie_vie_profile(marie_vie* h, int32_t prec, const void* x, void* 
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   return st;
+}
+
+marie_status marie_vie_autotune(marie_vie* h, int32_t prec, const void* x, void* y, int32_t nrhs, int32_t reps,
+                                int32_t* widths, double* ms, int32_t cap, int32_t* count, void* stream) {
+  if (!h || !x || !y || nrhs < 1 || reps < 1 || !count || (cap > 0 && (!widths || !ms))) {
+    set_error("marie_vie_autotune: invalid argument");
+    return MARIE_ERR_BAD_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (prec == MARIE_C64) {
+    if (!h->p32.built) { set_error("autotune: no complex64 state"); return MARIE_ERR_BAD_ARG; }
+    return autotune_state<float>(h, h->p32, x, y, nrhs, reps, s, widths, ms, cap, count);
+  }
+  if (prec != MARIE_C128) { set_error("prec must be MARIE_C128 or MARIE_C64"); return MARIE_ERR_BAD_ARG; }
+  if (c128_is_ff(h)) return autotune_state<ff>(h, h->pff, x, y, nrhs, reps, s, widths, ms, cap, count);
+  if (!h->p64.built) { set_error("autotune: no complex128 state"); return MARIE_ERR_BAD_ARG; }
+  return autotune_state<double>(h, h->p64, x, y, nrhs, reps, s, widths, ms, cap, count);
 }
 
 marie_status marie_vie_tiles(marie_vie* h, int32_t prec, int32_t* out) {

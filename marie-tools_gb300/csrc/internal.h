@@ -60,6 +60,7 @@ struct PrecState {
   cplx<T>* T1 = nullptr;      // ws_rhs * C * n3 * n2 * 2n1
   cplx<T>* S = nullptr;       // ws_rhs * C * 2n2 * n3 * 2n1
   int ws_rhs = 0;             // right-hand sides per matvec chunk
+  int ws_cap = 0;             // right-hand sides the work arrays hold (whole z-tile bundles)
   int TY = 1, TXY = 1, TX = 1;
 };
 

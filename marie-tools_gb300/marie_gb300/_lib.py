@@ -101,6 +101,8 @@ _PROTOS = {
                                              _vp]),
     "marie_vie_profile": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, ct.c_int32, c_double_p, _vp]),
     "marie_vie_tiles": (ct.c_int, [_vp, ct.c_int32, c_int32_p]),
+    "marie_vie_autotune": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, ct.c_int32, c_int32_p, c_double_p,
+                                      ct.c_int32, c_int32_p, _vp]),
     "marie_vie_release_workspace": (ct.c_int, [_vp]),
     "marie_vie_set_materials": (ct.c_int, [_vp, c_double_p]),
     "marie_vie_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64)]),

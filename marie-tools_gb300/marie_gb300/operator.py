@@ -185,6 +185,22 @@ class VieOperator:
                                           x.numel() // self.Nb, int(reps), _dptr(ms), self._stream()))
         return ms
 
+    def autotune(self, x, reps=3):
+        """Time mvp_vie on x (CUDA, nrhs*N_b; its dtype selects the precision)
+        for every z-pass tile width that fits, keep the fastest; returns
+        {width: mean ms}."""
+        import torch
+        prec = C128 if x.dtype == torch.complex128 else C64
+        x = x.contiguous()
+        y = torch.empty_like(x)
+        w = np.zeros(8, np.int32)
+        ms = np.zeros(8, np.float64)
+        cnt = np.zeros(1, np.int32)
+        check(self._lib.marie_vie_autotune(self._h, prec, ct.c_void_p(x.data_ptr()), ct.c_void_p(y.data_ptr()),
+                                           x.numel() // self.Nb, int(reps), w.ctypes.data_as(_lib.c_int32_p),
+                                           _dptr(ms), 8, cnt.ctypes.data_as(_lib.c_int32_p), self._stream()))
+        return {int(w[i]): float(ms[i]) for i in range(min(int(cnt[0]), 8))}
+
     def tiles(self, prec=C64):
         out = np.zeros(4, np.int32)
         check(self._lib.marie_vie_tiles(self._h, prec, out.ctypes.data_as(_lib.c_int32_p)))
