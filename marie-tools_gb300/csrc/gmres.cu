@@ -700,7 +700,8 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     MARIE_LAUNCH_CHECK();
     bool recomputed = false;
     if constexpr (std::is_same<T, float>::value) {
-      if (r_true && xs && m >= 2) {
+      static const bool recurrence = getenv("MARIE_INNER_RECURRENCE") && atoi(getenv("MARIE_INNER_RECURRENCE")) != 0;
+      if (r_true && xs && m >= 2 && !recurrence) {
         k_diff32<<<vgrid(Nb, nrhs), 256, 0, s>>>(x, xs, V + ld, vrs, Nb, d_mask);
         MARIE_LAUNCH_CHECK();
         MARIE_TRY(launch_matvec<float>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N, V + ld, vrs,
