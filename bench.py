@@ -198,7 +198,19 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
     green = U * (n + 1) ** 3 * s            # octant spectrum, read once per launch
     alg = units * per_rhs + green
     achieved = alg / (ms_z * 1e-3) / 1e9
+    # DRAM traffic of the launch: the ncu capture of k4_zp<6,PWL> on the 96^3
+    # ellipsoid with 4 right-hand sides (read + write bytes per launch, one
+    # kernel, `--metrics dram__bytes_read.sum,dram__bytes_write.sum`) set
+    # against the byte model of that launch (live slices read and written
+    # once, the full Green spectrum read once), and the same ratio applied to
+    # this launch's model.  A capture at this workload's size would hold tens
+    # of GB on the device.
     traffic = None
+    if wl["pwl"] and n % 16 == 0 and 16 <= n <= 128:
+        full = U * (2 * n) ** 3 * s                                     # full spectrum, pair layout
+        model = units * per_rhs + full
+        model96 = 4 * 8 * 96 ** 3 * 12 * 8 * Z96_LIVE + 60 * 192 ** 3 * 8
+        traffic = int(model * (Z96_DRAM_BYTES / model96))
     four_step = n % 16 == 0 and 16 <= n <= 128
     name = (f"k4_zp<{n // 16},{'PWL' if wl['pwl'] else 'PWC'}>" if four_step else "k_z<float>")
     # FP32 work of the same launch: per right-hand side and (kx, ky) column,
@@ -213,8 +225,17 @@ def roofline_z(op, wl, tiles, ms_z, peak, peak_kind, zfrac=1.0):
     return {"kernel": name + " (z FFT + Green block multiply + inverse z FFT)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "traffic": traffic, "alg_bytes_per_launch": int(alg), "launch_ms": round(ms_z, 4),
+            "traffic_source": ("ncu DRAM read+write of the same kernel on the 96^3 ellipsoid with 4 right-hand "
+                               "sides, scaled to this launch by its byte model (live slices once, full Green "
+                               "spectrum once)") if traffic else None,
             "units_per_launch": units, "peak_source": peak_kind,
             "fp32": {"flops_per_launch": int(flops), "achieved_tflops": round(flops / (ms_z * 1e-3) / 1e12, 2)}}
+
+
+# ncu, k4_zp<6,PWL> on the 96^3 ellipsoid (4 right-hand sides, live slice
+# fraction 0.9375): dram__bytes_read.sum + dram__bytes_write.sum per launch
+Z96_DRAM_BYTES = 4671918080 + 1248136960
+Z96_LIVE = 0.9375
 
 
 def run_ours(args, wl):
