@@ -15,6 +15,7 @@ namespace marie {
 
 static thread_local std::string t_err;
 std::atomic<int64_t> g_launches{0};
+thread_local int64_t t_launches = 0;
 
 void set_error(const char* fmt, ...) {
   char buf[1024];
@@ -45,7 +46,19 @@ marie_status dev_alloc(marie_vie* h, void** p, size_t bytes) {
   return MARIE_OK;
 }
 
+void graphs_free(marie_vie* h) {
+  for (auto& e : h->graphs)
+    if (e.second.exec) cudaGraphExecDestroy(e.second.exec);
+  h->graphs.clear();
+  if (h->gstream) cudaStreamDestroy(h->gstream);
+  for (auto& e : h->gev)
+    if (e) cudaEventDestroy(e);
+  h->gstream = nullptr;
+  h->gev[0] = h->gev[1] = nullptr;
+}
+
 void dev_free_all(marie_vie* h) {
+  graphs_free(h);
   for (void* p : h->allocs) cudaFree(p);
   h->allocs.clear();
   for (auto& e : h->gm_pool) cudaFree(e.first);
@@ -847,6 +860,7 @@ marie_status marie_vie_set_materials(marie_vie* h, const double* Mr_body) {
 marie_status marie_vie_release_workspace(marie_vie* h) {
   if (!h) { set_error("handle is NULL"); return MARIE_ERR_BAD_ARG; }
   cudaDeviceSynchronize();
+  graphs_free(h);     // they capture workspace pointers
   for (auto* pool : {&h->gm_pool, &h->io_pool}) {
     for (auto& e : *pool) {
       cudaFree(e.first);

@@ -570,6 +570,94 @@ static dim3 vgrid(int64_t Nb, int nrhs) {
   return dim3((unsigned)bx, (unsigned)nrhs);
 }
 
+// Every pointer and size an Arnoldi window's launches capture: a graph is
+// replayed only for an identical key.
+static std::vector<uint64_t> window_key(const marie_vie* h, size_t tsz, bool adjoint, int k0, int k1, int nrhs, int m,
+                                        int64_t Nb, const void* V, const GmState& st) {
+  return {(uint64_t)tsz, (uint64_t)adjoint, (uint64_t)k0, (uint64_t)k1, (uint64_t)nrhs, (uint64_t)m, (uint64_t)Nb,
+          (uint64_t)(uintptr_t)V, (uint64_t)(uintptr_t)st.H, (uint64_t)(uintptr_t)st.R, (uint64_t)(uintptr_t)st.cs,
+          (uint64_t)(uintptr_t)st.sn, (uint64_t)(uintptr_t)st.g, (uint64_t)(uintptr_t)st.y,
+          (uint64_t)(uintptr_t)st.res, (uint64_t)(uintptr_t)st.beta, (uint64_t)(uintptr_t)st.hnorm,
+          (uint64_t)(uintptr_t)st.resid, (uint64_t)(uintptr_t)st.tolabs, (uint64_t)(uintptr_t)st.kr,
+          (uint64_t)(uintptr_t)st.hist, (uint64_t)(uintptr_t)st.incyc, (uint64_t)(uintptr_t)st.part,
+          (uint64_t)(uintptr_t)st.npart, (uint64_t)(uintptr_t)h->hio, (uint64_t)h->hio_cap,
+          (uint64_t)h->p32.TX, (uint64_t)h->p64.TX, (uint64_t)h->pff.TX, (uint64_t)h->p32.ws_rhs,
+          (uint64_t)h->p64.ws_rhs, (uint64_t)h->pff.ws_rhs};
+}
+
+// MARIE_GMRES_GRAPH=0 turns the window graphs off.
+static bool graphs_enabled() {
+  static const bool v = [] {
+    const char* e = getenv("MARIE_GMRES_GRAPH");
+    return !(e && atoi(e) == 0);
+  }();
+  return v;
+}
+
+// Run an Arnoldi window: eagerly on `s` the first time its key is seen (this
+// also does the one-time set-up of the kernels it launches), captured into a
+// CUDA graph on the handle's own stream the second time, replayed from then
+// on.  The graph stream is joined to `s` by events both ways.  A capture that
+// fails leaves the window eager for good.
+template <typename F>
+static marie_status run_window(marie_vie* h, const std::vector<uint64_t>& key, F& window, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!graphs_enabled() || cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return window(s);
+  }
+  auto it = h->graphs.find(key);
+  if (it == h->graphs.end()) {
+    if (h->graphs.size() >= 4096) graphs_free(h);
+    h->graphs[key] = marie_vie::GraphEntry{};
+    return window(s);
+  }
+  marie_vie::GraphEntry& e = it->second;
+  if (e.kernels < 0) return window(s);
+  if (!h->gstream) {
+    if (cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->gev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->gev[1], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      e.kernels = -1;
+      return window(s);
+    }
+  }
+  MARIE_CUDA_TRY(cudaEventRecord(h->gev[0], s));
+  MARIE_CUDA_TRY(cudaStreamWaitEvent(h->gstream, h->gev[0], 0));
+  if (!e.exec) {
+    const int64_t before = t_launches;
+    if (cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      cudaGetLastError();
+      e.kernels = -1;
+      return window(s);
+    }
+    const marie_status st = window(h->gstream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(h->gstream, &g);
+    const int64_t nk = t_launches - before;
+    g_launches -= nk;     // captured, not run
+    t_launches -= nk;
+    cudaGraphExec_t ex = nullptr;
+    if (st != MARIE_OK || ce != cudaSuccess || !g || cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+      cudaGetLastError();
+      if (g) cudaGraphDestroy(g);
+      e.kernels = -1;
+      if (st != MARIE_OK) return st;
+      return window(s);
+    }
+    cudaGraphDestroy(g);
+    e.exec = ex;
+    e.kernels = nk;
+  }
+  MARIE_CUDA_TRY(cudaGraphLaunch(e.exec, h->gstream));
+  g_launches += e.kernels;
+  t_launches += e.kernels;
+  MARIE_CUDA_TRY(cudaEventRecord(h->gev[1], h->gstream));
+  MARIE_CUDA_TRY(cudaStreamWaitEvent(s, h->gev[1], 0));
+  return MARIE_OK;
+}
+
 struct RhsLog {
   std::vector<double> resvec;   // relative residual history
   int iters = 0, outer = 0, last_inner = 0, status = MARIE_OK;
@@ -651,29 +739,39 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     MARIE_LAUNCH_CHECK();
     for (int r = 0; r < nrhs; ++r) if (start[r]) log[r].outer = outit;
     incyc = start;
-    int k_win = 0;     // first step not yet logged
-    for (int k = 0; k < m; ++k) {
-      MARIE_TRY(launch_matvec<T>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N,
-                                 V + (int64_t)k * ld, vrs, V + (int64_t)(k + 1) * ld, vrs, nrhs, st.incyc, s));
-      ++*matvecs;
-      k_dots<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, st.incyc, st.part, nch);
-      MARIE_LAUNCH_CHECK();
-      k_reduce_dots<<<dim3((k + 8) / 8, nrhs), 256, 0, s>>>(st.part, nch, k, mp1, m, st.incyc, st.H);
-      MARIE_LAUNCH_CHECK();
-      k_update<T><<<cg, kVT, 0, s>>>(V, ld, Nb, k, mp1, m, st.incyc, st.H, st.npart, nch);
-      MARIE_LAUNCH_CHECK();
-      k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, st.incyc, st.hnorm);
-      MARIE_LAUNCH_CHECK();
-      // scale with the mask before the Givens step clears finished rhs
-      k_scale<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V + (int64_t)(k + 1) * ld, vrs, Nb, st.incyc, st.hnorm);
-      MARIE_LAUNCH_CHECK();
-      k_givens<<<sb, 128, 0, s>>>(st, k, m, nrhs);
-      MARIE_LAUNCH_CHECK();
-      if ((k + 1) % sync_steps() != 0 && k + 1 < m) continue;
+    // The Arnoldi steps run in windows of sync_steps() between host
+    // synchronisations; a window's launches (and the status reads that end
+    // it) replay as one CUDA graph from its second occurrence on.
+    for (int k0 = 0; k0 < m;) {
+      const int k1 = std::min(m, (k0 / sync_steps() + 1) * sync_steps());
+      auto window = [&](cudaStream_t q) -> marie_status {
+        for (int k = k0; k < k1; ++k) {
+          MARIE_TRY(launch_matvec<T>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N,
+                                     V + (int64_t)k * ld, vrs, V + (int64_t)(k + 1) * ld, vrs, nrhs, st.incyc, q));
+          k_dots<T><<<cg, kVT, 0, q>>>(V, ld, Nb, k, mp1, st.incyc, st.part, nch);
+          MARIE_LAUNCH_CHECK();
+          k_reduce_dots<<<dim3((k + 8) / 8, nrhs), 256, 0, q>>>(st.part, nch, k, mp1, m, st.incyc, st.H);
+          MARIE_LAUNCH_CHECK();
+          k_update<T><<<cg, kVT, 0, q>>>(V, ld, Nb, k, mp1, m, st.incyc, st.H, st.npart, nch);
+          MARIE_LAUNCH_CHECK();
+          k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, q>>>(st.npart, nch, nrhs, st.incyc, st.hnorm);
+          MARIE_LAUNCH_CHECK();
+          // scale with the mask before the Givens step clears finished rhs
+          k_scale<T><<<vgrid(Nb, nrhs), 256, 0, q>>>(V + (int64_t)(k + 1) * ld, vrs, Nb, st.incyc, st.hnorm);
+          MARIE_LAUNCH_CHECK();
+          k_givens<<<sb, 128, 0, q>>>(st, k, m, nrhs);
+          MARIE_LAUNCH_CHECK();
+        }
+        MARIE_TRY(chan_get(h, SLOT_INCYC, nrhs, st.incyc, nrhs, q));
+        MARIE_TRY(chan_get(h, SLOT_KR, nrhs, st.kr, nrhs * sizeof(int), q));
+        MARIE_TRY(chan_get_hist(h, nrhs, st.hist, (size_t)nrhs * m * sizeof(double), q));
+        return MARIE_OK;
+      };
+      MARIE_TRY(chan_reserve(h, nrhs));
+      const std::vector<uint64_t> key = window_key(h, sizeof(T), sc.adjoint, k0, k1, nrhs, m, Nb, V, st);
+      MARIE_TRY(run_window(h, key, window, s));
+      *matvecs += k1 - k0;
       prev = incyc;
-      MARIE_TRY(chan_get(h, SLOT_INCYC, nrhs, st.incyc, nrhs, s));
-      MARIE_TRY(chan_get(h, SLOT_KR, nrhs, st.kr, nrhs * sizeof(int), s));
-      MARIE_TRY(chan_get_hist(h, nrhs, st.hist, (size_t)nrhs * m * sizeof(double), s));
       MARIE_CUDA_TRY(cudaStreamSynchronize(s));
       chan_take(h, SLOT_INCYC, nrhs, incyc.data(), nrhs);
       chan_take(h, SLOT_KR, nrhs, kr.data(), nrhs * sizeof(int));
@@ -681,14 +779,14 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
       int any = 0;
       for (int r = 0; r < nrhs; ++r) {
         if (!prev[r]) continue;
-        // steps [k_win, kr) of this window ran for r
-        for (int j = k_win; j < kr[r]; ++j) {
+        // steps [k0, kr) of this window ran for r
+        for (int j = k0; j < kr[r]; ++j) {
           log[r].resvec.push_back(hist[(size_t)r * m + j] / bnorm[r]);
           log[r].iters++;
         }
         if (incyc[r]) any = 1;
       }
-      k_win = k + 1;
+      k0 = k1;
       if (!any) break;
     }
     // finalize the cycle of every rhs that ran it

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <atomic>
+#include <map>
 #include <utility>
 #include <string>
 #include <vector>
@@ -15,6 +16,7 @@ namespace marie {
 
 void set_error(const char* fmt, ...);
 extern std::atomic<int64_t> g_launches;
+extern thread_local int64_t t_launches;   // this thread's share of g_launches
 
 #define MARIE_CUDA_TRY(expr)                                                             \
   do {                                                                                   \
@@ -29,6 +31,7 @@ extern std::atomic<int64_t> g_launches;
 #define MARIE_LAUNCH_CHECK()                 \
   do {                                       \
     ::marie::g_launches.fetch_add(1);        \
+    ++::marie::t_launches;                   \
     MARIE_CUDA_TRY(cudaGetLastError());      \
   } while (0)
 
@@ -120,12 +123,23 @@ struct marie_vie {
   // engine behind the chunk copies of the host-buffer solve.
   unsigned char* hio = nullptr;
   size_t hio_cap = 0;
+  // CUDA graphs of Arnoldi windows (the launches between two host
+  // synchronisations of the GMRES loop), keyed by every pointer and size the
+  // launches capture; replayed by later cycles and solves of the same shape.
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int64_t kernels = 0;
+  };
+  std::map<std::vector<uint64_t>, GraphEntry> graphs;
+  cudaStream_t gstream = nullptr;    // the graphs run here, joined to the caller's stream by events
+  cudaEvent_t gev[2] = {nullptr, nullptr};
 };
 
 namespace marie {
 
 marie_status dev_alloc(marie_vie* h, void** p, size_t bytes);
 void dev_free_all(marie_vie* h);
+void graphs_free(marie_vie* h);
 
 enum OpKind { OP_N = 0, OP_N_ADJ = 1, OP_K = 2, OP_K_ADJ = 3 };
 
