@@ -395,30 +395,6 @@ __global__ void k_convert(const cplx<Ti>* src, int64_t srs, cplx<To>* dst, int64
     d[i] = cplx<To>{(To)s[i].x, (To)s[i].y};
 }
 
-// Restart residual of the inner complex64 solve, recomputed instead of the
-// recurrence V (beta e1 - H y): d = c64(x - xs) (the correction since the
-// refinement step began) into one basis slot, then r = c64(r64 - A32 d).
-__global__ void k_diff32(const zd* x, const zd* xs, cplx<float>* d, int64_t drs, int64_t Nb,
-                         const unsigned char* act) {
-  const int r = blockIdx.y;
-  if (!act[r]) return;
-  const zd* a = x + (int64_t)r * Nb;
-  const zd* b = xs + (int64_t)r * Nb;
-  cplx<float>* o = d + (int64_t)r * drs;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x)
-    o[i] = cplx<float>{(float)(a[i].x - b[i].x), (float)(a[i].y - b[i].y)};
-}
-__global__ void k_rtrue32(const zd* r64, const cplx<float>* ad, int64_t ars, cplx<float>* v, int64_t vrs, int64_t Nb,
-                          const unsigned char* act) {
-  const int r = blockIdx.y;
-  if (!act[r]) return;
-  const zd* a = r64 + (int64_t)r * Nb;
-  const cplx<float>* b = ad + (int64_t)r * ars;
-  cplx<float>* o = v + (int64_t)r * vrs;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Nb; i += (int64_t)gridDim.x * blockDim.x)
-    o[i] = cplx<float>{(float)(a[i].x - (double)b[i].x), (float)(a[i].y - (double)b[i].y)};
-}
-
 // r = b - r  (r holds A x on entry); FP64
 __global__ void k_residual(const zd* b, zd* r, int64_t Nb, const unsigned char* act) {
   const int k = blockIdx.y;
@@ -666,17 +642,10 @@ struct RhsLog {
 // Run restarted GMRES on A_T for all rhs with todo[r] != 0.  On entry V_0 of
 // each such rhs holds its initial residual r0 (unnormalised); bnorm[r] is the
 // reference norm for the relative tolerance.  x (FP64) receives += V y.
-// r_true / xs (complex64 inner solves of the mixed mode only): the FP64
-// residual the inner problem A d = r_true starts from, and x at that start;
-// with them every restart takes the residual r_true - A (x - xs) computed
-// by a complex64 matvec instead of the recurrence, whose drift in FP32 over
-// several cycles would otherwise leave the true residual several times above
-// the inner target and cost another refinement step.
 template <typename T>
 static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x, const std::vector<double>& bnorm,
                                const std::vector<double>& tolrel, int maxit, const std::vector<unsigned char>& todo,
-                               std::vector<RhsLog>& log, int* matvecs, cudaStream_t s, Scratch& sc,
-                               const zd* r_true = nullptr, const zd* xs = nullptr) {
+                               std::vector<RhsLog>& log, int* matvecs, cudaStream_t s, Scratch& sc) {
   const int64_t Nb = h->Nb;
   const int mp1 = m + 1;
   const int nch = (int)((Nb + kCH - 1) / kCH);
@@ -796,24 +765,8 @@ static marie_status gmres_core(marie_vie* h, int nrhs, cplx<T>* V, int m, zd* x,
     MARIE_LAUNCH_CHECK();
     k_xupdate<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, ld, mp1, m, Nb, d_mask, st, x, Nb);
     MARIE_LAUNCH_CHECK();
-    bool recomputed = false;
-    if constexpr (std::is_same<T, float>::value) {
-      static const bool recurrence = getenv("MARIE_INNER_RECURRENCE") && atoi(getenv("MARIE_INNER_RECURRENCE")) != 0;
-      if (r_true && xs && m >= 2 && !recurrence) {
-        k_diff32<<<vgrid(Nb, nrhs), 256, 0, s>>>(x, xs, V + ld, vrs, Nb, d_mask);
-        MARIE_LAUNCH_CHECK();
-        MARIE_TRY(launch_matvec<float>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N, V + ld, vrs,
-                                       V + 2 * ld, vrs, nrhs, d_mask, s));
-        ++*matvecs;
-        k_rtrue32<<<vgrid(Nb, nrhs), 256, 0, s>>>(r_true, V + 2 * ld, vrs, V, vrs, Nb, d_mask);
-        MARIE_LAUNCH_CHECK();
-        recomputed = true;
-      }
-    }
-    if (!recomputed) {
-      k_rform<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, ld, mp1, Nb, d_mask, st);
-      MARIE_LAUNCH_CHECK();
-    }
+    k_rform<T><<<vgrid(Nb, nrhs), 256, 0, s>>>(V, ld, mp1, Nb, d_mask, st);
+    MARIE_LAUNCH_CHECK();
     k_norm2<T><<<cg, kVT, 0, s>>>(V, vrs, Nb, d_mask, st.npart, nch);
     MARIE_LAUNCH_CHECK();
     k_reduce_norm<<<(nrhs + 7) / 8, 256, 0, s>>>(st.npart, nch, nrhs, d_mask, st.beta);
@@ -959,8 +912,6 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
   } else {
     cplx<float>* V = nullptr;
     MARIE_TRY(sc.get(&V, (size_t)nrhs * (m + 1) * Nb));
-    zd* xs = nullptr;     // x at the start of each refinement step
-    MARIE_TRY(sc.get(&xs, (size_t)nrhs * Nb));
     std::vector<double> rel(nrhs, 1.0);
     if (o->x0_present) {
       MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, rel, &mv64, s, sc));
@@ -997,10 +948,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
         tin[r] = std::min(0.5, std::max(floor_tol, safety * o->tol / std::max(rel[r], 1e-300)));
       }
       std::vector<RhsLog> ilog(nrhs);
-      k_convert<double, double><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)x, Nb, (cplx<double>*)xs, Nb, Nb,
-                                                                d_todo);
-      MARIE_LAUNCH_CHECK();
-      MARIE_TRY(gmres_core<float>(h, nrhs, V, m, x, rn, tin, o->maxit, todo, ilog, &mv32, s, sc, r64, xs));
+      MARIE_TRY(gmres_core<float>(h, nrhs, V, m, x, rn, tin, o->maxit, todo, ilog, &mv32, s, sc));
       for (int r = 0; r < nrhs; ++r) {
         if (!todo[r]) continue;
         log[r].iters += ilog[r].iters;

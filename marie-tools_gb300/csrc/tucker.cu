@@ -51,25 +51,49 @@ __global__ void k_tkf2(const cplx<float>* __restrict__ P1, const cplx<float>* __
   }
 }
 
-// One thread per (ky, kx, k): the pair (2k, 2k+1) of the column, all of U1's
-// rank inner products, written as one 16-byte entry.
-__global__ void k_tkf3(const cplx<float>* __restrict__ P2, const cplx<float>* __restrict__ U1, float4* dst, int r1,
-                       int m1, int m2, int n3, int U, int blk, float scl) {
-  const int64_t total = (int64_t)m2 * m1 * n3;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(i % n3);
-    const int64_t col = i / n3;          // ky * m1 + kx
-    const int kx = (int)(col % m1);
-    const int ky = (int)(col / m1);
-    const cplx<float>* p0 = P2 + (int64_t)r1 * (ky + (int64_t)m2 * (2 * k));
-    const cplx<float>* p1 = p0 + (int64_t)r1 * m2;
-    const cplx<float>* u = U1 + (int64_t)r1 * kx;
-    cplx<float> g0{0.f, 0.f}, g1{0.f, 0.f};
-    for (int a = 0; a < r1; ++a) {
-      fma_c(g0, p0[a], u[a]);
-      fma_c(g1, p1[a], u[a]);
+// The last mode product is, for each ky, the product of U1^T (2n1 x r1)
+// with the slab P2[:, ky, :] (r1 x 2n3).  A CTA takes one (ky, block) and a
+// tile of kTkX consecutive kx: its threads run over the frequency pairs k
+// (coalesced 16-byte stores), each holding the slab's two rank vectors for
+// its pair in registers, with the tile's U1 columns staged in shared
+// memory and read as broadcasts.
+constexpr int kTkX = 16;
+constexpr int kTkMaxR = 32;     // largest r1 of the per-application mode (checked at create)
+__global__ void __launch_bounds__(128) k_tkf3(const cplx<float>* __restrict__ P2, const cplx<float>* __restrict__ U1,
+                                              float4* dst, int r1, int m1, int m2, int n3, int U, int blk, float scl) {
+  __shared__ cplx<float> u[kTkMaxR * kTkX];
+  const int ky = blockIdx.y;
+  const int kx0 = blockIdx.x * kTkX;
+  const int nkx = min(kTkX, m1 - kx0);
+  for (int i = threadIdx.x; i < r1 * nkx; i += blockDim.x) {
+    const int a = i % r1, j = i / r1;
+    u[j * kTkMaxR + a] = U1[a + (int64_t)r1 * (kx0 + j)];
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n3; k += blockDim.x) {
+    cplx<float> p0[kTkMaxR], p1[kTkMaxR];
+    const cplx<float>* q0 = P2 + (int64_t)r1 * (ky + (int64_t)m2 * (2 * k));
+    const cplx<float>* q1 = q0 + (int64_t)r1 * m2;
+#pragma unroll
+    for (int a = 0; a < kTkMaxR; ++a) {
+      if (a < r1) {
+        p0[a] = q0[a];
+        p1[a] = q1[a];
+      }
     }
-    dst[(col * U + blk) * n3 + k] = make_float4(g0.x * scl, g1.x * scl, g0.y * scl, g1.y * scl);
+    for (int j = 0; j < nkx; ++j) {
+      cplx<float> g0{0.f, 0.f}, g1{0.f, 0.f};
+      const cplx<float>* uj = u + j * kTkMaxR;
+#pragma unroll
+      for (int a = 0; a < kTkMaxR; ++a) {
+        if (a < r1) {
+          fma_c(g0, p0[a], uj[a]);
+          fma_c(g1, p1[a], uj[a]);
+        }
+      }
+      const int64_t col = (int64_t)ky * m1 + kx0 + j;
+      dst[(col * U + blk) * n3 + k] = make_float4(g0.x * scl, g1.x * scl, g0.y * scl, g1.y * scl);
+    }
   }
 }
 
@@ -88,6 +112,10 @@ marie_status tucker_keep_c64(marie_vie* h, const marie_tucker_block* tk) {
   const int m1 = 2 * h->n1, m2 = 2 * h->n2, m3 = 2 * h->n3;
   for (int id = 0; id < nblk; ++id) {
     const marie_tucker_block& b = tk[id];
+    if (b.r1 > kTkMaxR) {
+      set_error("per-application Tucker expansion: block %d has rank r1 = %d above %d", id, b.r1, kTkMaxR);
+      return MARIE_ERR_NOT_SUPPORTED;
+    }
     TuckerDev::Block& d = t.blocks[id];
     d.r1 = b.r1;
     d.r2 = b.r2;
@@ -126,7 +154,8 @@ marie_status tucker_expand_c64(marie_vie* h, cudaStream_t s) {
     MARIE_LAUNCH_CHECK();
     k_tkf2<<<grid_of((int64_t)b.r1 * m2 * m3), 256, 0, s>>>(t.P1, b.U2, t.P2, b.r1, b.r2, m2, m3);
     MARIE_LAUNCH_CHECK();
-    k_tkf3<<<grid_of((int64_t)m2 * m1 * n3), 256, 0, s>>>(t.P2, b.U1, dst, b.r1, m1, m2, n3, U, id, scl);
+    k_tkf3<<<dim3((unsigned)((m1 + kTkX - 1) / kTkX), (unsigned)m2), 128, 0, s>>>(t.P2, b.U1, dst, b.r1, m1, m2, n3,
+                                                                                U, id, scl);
     MARIE_LAUNCH_CHECK();
   }
   return MARIE_OK;
