@@ -22,6 +22,12 @@
 
 namespace marie {
 
+// Bulk prefetch of [p, p + bytes) into L2 (no data returned to the SM);
+// p and bytes multiples of 16.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ cp lds_cp(const cp* p) {
   const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p);
   return cp{f2{v.x}, f2{v.y}};
@@ -166,6 +172,23 @@ __global__ void __launch_bounds__(kZpThreads, 2) k4_zp(MvArgs<float> a) {
     tw2s[i] = make_float2(t2.x, t2.y);
   }
   if (threadIdx.x < NB) zqs[threadIdx.x] = a.zq ? a.zq[threadIdx.x] : 0xffffu;
+  // The first bundle of a column starts its Green rows (U blocks x N pairs
+  // x 16 bytes, contiguous per column) on their way to L2 while the forward
+  // transforms run, so the product finds them there instead of in HBM; the
+  // other bundles of the column run right after it and share them.
+  if (bu == 0) {
+    const int pb = kyp / n2, pky = 2 * (kyp - pb * n2) + pb;
+    const int ncol = min(a.TX, m1 - k0);
+    const int64_t colb = (int64_t)U * N * 16;
+    const unsigned piece = (unsigned)(colb / 8);      // U * N * 2 bytes: a multiple of 16
+    for (int c = threadIdx.x; c < ncol * 8; c += blockDim.x) {
+      const int kxp = k0 + (c >> 3);
+      const int pa = kxp >= n1 ? 1 : 0;
+      const int pkx = 2 * (kxp - pa * n1) + pa;
+      const char* col = reinterpret_cast<const char*>(a.G) + ((int64_t)pky * m1 + pkx) * colb;
+      prefetch_l2_bulk(col + (int64_t)(c & 7) * piece, piece);
+    }
+  }
   __syncthreads();
   const int64_t row = (int64_t)m1 * R;
   const int64_t cstride = (int64_t)2 * n2 * N * row;
