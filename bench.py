@@ -2,7 +2,8 @@
 
 Workload (default): ellipsoid phantom on a 128^3 grid at 2 mm, PWL basis
 (12 unknowns/voxel), 297.2 MHz, 64 right-hand sides from 64 loop ports on a
-16 cm cylinder; complex64 GMRES(50) with FP32 accumulation inside an FP64
+16 cm cylinder; Green's tensor with the accurate near zone (the reference's
+operator); complex64 GMRES(50) with FP32 accumulation inside an FP64
 iterative-refinement loop to 1e-6 relative residual.  One step = one batched
 solve of all right-hand sides, inputs resident in HBM.
 
@@ -11,7 +12,10 @@ solve of all right-hand sides, inputs resident in HBM.
 Other workloads (--workload): sphere32 (r = 6 cm sphere, 32^3 at 5 mm, PWC,
 128 MHz, plane wave), ellipsoid96 (the phantom on 96^3 at 2 mm, PWL, one
 loop) and uneven16 (sixteen PWC phantoms with edges 48-128 and 1-8 loops
-each, solved body after body; reports the per-body residual spread).
+each, the bodies on concurrent streams; reports the per-body residual
+spread).  --matvec-only times operator applications alone (the small,
+bounded command of the ncu captures), optionally from Tucker blocks
+(--tucker pre|apply).
 
 Under torchrun each rank solves its own batch (replicas of the workload with
 rank-seeded loop jitter; no collective on the data path), value = solves of
