@@ -172,11 +172,14 @@ __global__ void __launch_bounds__(kZpThreads, 2) k4_zp(MvArgs<float> a) {
     tw2s[i] = make_float2(t2.x, t2.y);
   }
   if (threadIdx.x < NB) zqs[threadIdx.x] = a.zq ? a.zq[threadIdx.x] : 0xffffu;
-  // The first bundle of a column starts its Green rows (U blocks x N pairs
-  // x 16 bytes, contiguous per column) on their way to L2 while the forward
-  // transforms run, so the product finds them there instead of in HBM; the
-  // other bundles of the column run right after it and share them.
-  if (bu == 0) {
+  // When several bundles share a column, the first starts the column's
+  // Green rows (U blocks x N pairs x 16 bytes, contiguous per column) on
+  // their way to L2 while the forward transforms run, so the product finds
+  // them there instead of in HBM; the other bundles of the column run right
+  // after it and share them.  (With one bundle the prefetch only competes
+  // with the step-1 loads: measured 23% slower at 96^3 with one
+  // right-hand side.)
+  if (bu == 0 && gridDim.x > 1) {
     const int pb = kyp / n2, pky = 2 * (kyp - pb * n2) + pb;
     const int ncol = min(a.TX, m1 - k0);
     const int64_t colb = (int64_t)U * N * 16;
