@@ -49,6 +49,7 @@ WORKLOADS = {
                  fp64_iters=66.0, desc="sphere r=6 cm 32^3 @ 5 mm, PWC, 128 MHz, plane wave"),
 }
 METRIC = "GMRES solves/s at 128^3 PWL, 1e-6 resid (mixed c64/FP64-refined, 64-RHS batch)"
+BLOCK_STEPS = 30     # block Arnoldi steps per cycle of the block solver
 
 
 def metric_of(wl):
@@ -169,23 +170,33 @@ def build_problem(wl, rank, torch):
     return op, body, b.reshape(-1), t_asm
 
 
-def solve_alg_bytes(n, pwl, Nb, iters, n_c128, chunk, restart=50):
+def solve_alg_bytes(n, pwl, Nb, iters, n_c128, chunk, restart=50, block_steps=0, cycles=None):
     """Algorithmic bytes of one batched mixed solve by the fixed per-matvec
     and per-Arnoldi-step formulas: per right-hand side, `iters[r]` complex64
     matvecs of 26 n^3 C s bytes plus the Green spectrum U (n+1)^3 s shared by
-    the `chunk` right-hand sides of a launch, Arnoldi step k of a cycle
-    (2k + 4) N_b s bytes, and `n_c128` complex128 true-residual matvecs
-    (s = 16)."""
+    the `chunk` right-hand sides of a launch, and `n_c128` complex128
+    true-residual matvecs (s = 16).  Per-RHS GMRES: Arnoldi step k of a cycle
+    (2k + 4) N_b s bytes.  Block GMRES (block_steps > 0, `cycles[r]` cycles):
+    block step j reads V_{0:j} twice (projection, update; (j+1) vectors per
+    right-hand side each) and W six times (update, two Gram matrices, two
+    normalisations, the copy) and writes it four times: (2(j+1) + 10) N_b s
+    per right-hand side."""
     C, U = (12, 60) if pwl else (3, 6)
 
     def mv(s):
         return 26 * n ** 3 * C * s + U * (n + 1) ** 3 * s / chunk
 
     total = 0.0
-    for it in np.asarray(iters, dtype=np.int64).reshape(-1):
+    its = np.asarray(iters, dtype=np.int64).reshape(-1)
+    for r, it in enumerate(its):
         it = int(it)
-        full, rem = divmod(it, restart)
-        steps = full * (restart * (restart + 1) + 4 * restart) + rem * (rem + 1) + 4 * rem   # sum of (2k + 4)
+        if block_steps > 0:
+            ncyc = max(1, int(cycles[r]))
+            per = it / ncyc           # steps of a cycle (the cycles' mean)
+            steps = ncyc * sum(2 * (j + 1) + 10 for j in range(int(round(per))))
+        else:
+            full, rem = divmod(it, restart)
+            steps = full * (restart * (restart + 1) + 4 * restart) + rem * (rem + 1) + 4 * rem   # sum of (2k + 4)
         total += it * mv(8) + steps * Nb * 8 + n_c128 * mv(16)
     return total
 
@@ -258,7 +269,11 @@ def run_ours(args, wl):
     ge.build()
     op, body, b, t_asm = build_problem(wl, rank, torch)
     nrhs = wl["nrhs"]
-    kw = dict(restart=50, tol=wl["tol"], maxit=200, mode="mixed", inner_tol=1e-7)
+    # the right-hand sides of a batch share one block Krylov space (block
+    # GMRES, 30 block steps per cycle); one right-hand side runs the
+    # per-RHS mixed solver
+    solver = args.solver or ("block" if nrhs >= 8 else "mixed")
+    kw = dict(restart=50, tol=wl["tol"], maxit=200, mode=solver, inner_tol=1e-7, block_steps=BLOCK_STEPS)
     # warm-up (also the solve whose statistics are reported)
     rep = None
     for _ in range(args.warmup):
@@ -285,8 +300,9 @@ def run_ours(args, wl):
     value = nrhs * args.steps * ws / (ms_max * 1e-3)
 
     # end to end through the public API on host buffers (marie_gmres_vie_host:
-    # pinned b in, x out, copies inside the timed region, overlapped with the
-    # chunked solve)
+    # pinned b in, x out, copies inside the timed region; the per-RHS solver
+    # overlaps them with its chunks, the block solver takes the whole batch
+    # as one block)
     b_host = b.cpu().pin_memory()
     x_host = torch.empty_like(b_host).pin_memory()
     # warm-up of the host path's own device buffers: a loose tolerance ends
@@ -348,6 +364,24 @@ def run_ours(args, wl):
                 "mixed_over_fp64": round(ms_64 / ms_m, 3),
                 "field_err_mixed_vs_fp64_max": float(ferr.max())}
 
+    # the per-right-hand-side mixed solver on the same batch, for comparison
+    per_rhs = None
+    if solver == "block" and not args.skip_fp64:
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        g0.record(stream)
+        xp, repp = op.gmres(b, **dict(kw, mode="mixed"))
+        g1.record(stream)
+        torch.cuda.synchronize()
+        ms_p = g0.elapsed_time(g1)
+        XB, XP = x.reshape(nrhs, op.Nb), xp.reshape(nrhs, op.Nb)
+        dif = (torch.linalg.norm(XB - XP, dim=1) / torch.linalg.norm(XP, dim=1)).cpu().numpy()
+        per_rhs = {"solver": "complex64 GMRES(50) per right-hand side + FP64 refinement", "batch_rhs": nrhs,
+                   "solves_per_s": round(nrhs / (ms_p * 1e-3), 4), "iters_mean": float(np.mean(repp.iters)),
+                   "matvecs_c64": int(repp.matvecs_c64), "true_resid_max": float(repp.true_resid.max()),
+                   "block_over_per_rhs": round(ms_p / (ms_max / args.steps), 3),
+                   "solution_diff_max": float(dif.max())}
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = cpu_baseline(wl, iters=(fp64["iters_mean"] if fp64 else wl["fp64_iters"]), budget_s=args.cpu_budget)
@@ -361,12 +395,14 @@ def run_ours(args, wl):
     # whole-solve bytes by the fixed formulas over the measured step time
     try:
         alg = solve_alg_bytes(wl["n"], wl["pwl"], op.Nb, rep.iters, int(rep.matvecs_c128),
-                              min(nrhs, tiles["chunk"]))
+                              min(nrhs, tiles["chunk"]), block_steps=BLOCK_STEPS if solver == "block" else 0,
+                              cycles=rep.outer)
         solve_roofline = {"bound": "hbm", "alg_bytes_per_step": int(alg),
                           "achieved": round(alg / (ms_max / args.steps * 1e-3) / 1e9, 1), "unit": "GB/s",
                           "peak": peak, "frac": round(alg / (ms_max / args.steps * 1e-3) / 1e9 / peak, 4),
                           "peak_source": peak_kind,
-                          "model": "per RHS: iters x c64 matvec (26 n^3 C 8 B + Green/chunk) + sum_k (2k+4) N_b 8 B "
+                          "model": "per RHS: iters x c64 matvec (26 n^3 C 8 B + Green/chunk) + Arnoldi bytes "
+                                   "(per-RHS: sum_k (2k+4) N_b 8 B; block: sum_j (2(j+1)+10) N_b 8 B) "
                                    "+ c128 residual matvecs (16 B)"}
     except Exception as e:      # a reported extra: never fail the run over it
         solve_roofline = {"error": repr(e)}
@@ -379,7 +415,10 @@ def run_ours(args, wl):
             "config": {"workload": wl["desc"], "grid": [wl["n"]] * 3, "basis": "PWL" if wl["pwl"] else "PWC",
                        "near_zone": wl.get("near", "relative"),
                        "n_body_voxels": int(body.idxS.size), "unknowns_per_rhs": int(op.Nb),
-                       "rhs_per_gpu": nrhs, "restart": 50, "tol": wl["tol"],
+                       "rhs_per_gpu": nrhs, "tol": wl["tol"],
+                       "solver": (f"block GMRES, {BLOCK_STEPS} block steps per cycle, one block of {nrhs} RHS, "
+                                  "FP64 refinement" if solver == "block" else
+                                  "complex64 GMRES(50) per RHS, FP64 refinement"),
                        "l2": "inputs larger than L2 (Krylov basis and FFT work arrays are tens of GB)",
                        "parallelism": f"replicas x{ws} (independent RHS batches, no collective)"},
             "e2e": e2e, "gpu_launches": int(launches),
@@ -387,7 +426,7 @@ def run_ours(args, wl):
             "solve": {"iters_per_rhs_mean": float(np.mean(rep.iters)), "matvecs_c64": int(rep.matvecs_c64),
                       "matvecs_c128": int(rep.matvecs_c128), "true_resid_max": float(np.max(rep.true_resid)),
                       "converged": int(np.sum(rep.status == 0))},
-            "fp64_gpu": fp64, "assembly_s": round(t_asm, 2),
+            "fp64_gpu": fp64, "per_rhs_mixed": per_rhs, "assembly_s": round(t_asm, 2),
             "solve_roofline": solve_roofline,
         }
         print(json.dumps(line), flush=True)
@@ -657,6 +696,8 @@ def main():
     ap.add_argument("--tucker", default="none", choices=["none", "pre", "apply"],
                     help="--matvec-only: build the operator from Tucker blocks (tolerance 1e-7) expanded once at "
                          "create (pre) or re-expanded in every complex64 application (apply)")
+    ap.add_argument("--solver", default=None, choices=["block", "mixed"],
+                    help="inner solver (default: block for batches of 8 or more right-hand sides)")
     ap.add_argument("--prec", default="c64", choices=["c64", "c128", "c128ff"],
                     help="precision of --matvec-only (c128ff: complex128 in float-float arithmetic)")
     args = ap.parse_args()

@@ -131,11 +131,14 @@ marie_status marie_vie_apply_N_noalloc(int32_t n1, int32_t n2, int32_t n3, int32
 
 typedef enum {
   MARIE_SOLVE_FP64 = 0,   /* complex128 GMRES, faithful to is_gmres_vie.m */
-  MARIE_SOLVE_MIXED = 1   /* complex64 GMRES inside an FP64 iterative-refinement loop */
+  MARIE_SOLVE_MIXED = 1,  /* complex64 GMRES inside an FP64 iterative-refinement loop */
+  MARIE_SOLVE_MIXED_BLOCK = 2  /* MIXED with one block Krylov space shared by the right-hand
+                                  sides of each refinement step (block GMRES, block_steps
+                                  block Arnoldi steps per cycle, maxit cycles) */
 } marie_solve_mode;
 
 typedef struct {
-  int32_t restart;        /* is_gmres_vie restart (reference: 50) */
+  int32_t restart;        /* is_gmres_vie restart (reference: 50), 1..128 */
   int32_t maxit;          /* max restart cycles (reference: 200) */
   double tol;             /* relative residual target */
   int32_t mode;           /* marie_solve_mode */
@@ -147,6 +150,8 @@ typedef struct {
                              the FP64 true residual decides convergence either way */
   int32_t adjoint;        /* 1: solve A^H x = b (A^H as marie_vie_apply_adjoint), for adjoint
                              sensitivities; 0: A x = b */
+  int32_t block_steps;    /* MIXED_BLOCK: block Arnoldi steps per cycle (0 = 20); the block
+                             basis holds (block_steps+1) x nrhs complex64 vectors */
 } marie_gmres_opts;
 
 typedef struct {

@@ -68,6 +68,10 @@ void dev_free_all(marie_vie* h) {
   if (h->hio) cudaFreeHost(h->hio);
   h->hio = nullptr;
   h->hio_cap = 0;
+  if (h->bio) cudaFreeHost(h->bio);
+  h->bio = nullptr;
+  h->bio_cap = 0;
+  blas_free(h);
   h->mem_used = 0;
 }
 

@@ -20,7 +20,7 @@
 
 namespace marie {
 
-constexpr int kMaxRestart = 64;   // largest GMRES restart length
+constexpr int kMaxRestart = 128;  // largest GMRES restart length
 
 
 typedef cplx<double> zd;
@@ -126,7 +126,7 @@ template <typename T>
 __global__ void k_update(cplx<T>* V, int64_t ld, int64_t Nb, int k, int mp1, int m, const unsigned char* act,
                          const zd* H, double* npart, int nch) {
   typedef typename Acc<T>::type A;
-  __shared__ cplx<T> hs[64];
+  __shared__ cplx<T> hs[kMaxRestart];
   __shared__ cplx<A> sh[32];
   const int r = blockIdx.y;
   if (!act[r]) return;
@@ -837,6 +837,12 @@ static marie_status norms(marie_vie* h, int nrhs, const zd* v, std::vector<doubl
   return MARIE_OK;
 }
 
+}  // namespace marie
+
+#include "bgmres.cuh"
+
+namespace marie {
+
 static void fill_report(marie_gmres_report* rep, const std::vector<RhsLog>& log, const std::vector<double>& trel,
                         int mv64, int mv32) {
   if (!rep) return;
@@ -868,12 +874,16 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
   if (o->restart < 1 || o->restart > kMaxRestart) { set_error("restart must be in [1, %d]", kMaxRestart); return MARIE_ERR_BAD_ARG; }
   if (o->maxit < 0) { set_error("maxit must be >= 0"); return MARIE_ERR_BAD_ARG; }
   if (!(o->tol > 0)) { set_error("tol must be > 0"); return MARIE_ERR_BAD_ARG; }
-  if (o->mode != MARIE_SOLVE_FP64 && o->mode != MARIE_SOLVE_MIXED) { set_error("unknown solve mode"); return MARIE_ERR_BAD_ARG; }
+  if (o->mode != MARIE_SOLVE_FP64 && o->mode != MARIE_SOLVE_MIXED && o->mode != MARIE_SOLVE_MIXED_BLOCK) {
+    set_error("unknown solve mode");
+    return MARIE_ERR_BAD_ARG;
+  }
+  if (o->block_steps < 0 || o->block_steps > 200) { set_error("block_steps must be in [0, 200]"); return MARIE_ERR_BAD_ARG; }
   if (!h->p64.built && !h->pff.built) {
     set_error("GMRES needs a complex128 operator (precisions bit 1 or 4)");
     return MARIE_ERR_BAD_ARG;
   }
-  if (o->mode == MARIE_SOLVE_MIXED && !h->p32.built) { set_error("mixed mode needs the complex64 operator (precisions bit 2)"); return MARIE_ERR_BAD_ARG; }
+  if (o->mode != MARIE_SOLVE_FP64 && !h->p32.built) { set_error("mixed mode needs the complex64 operator (precisions bit 2)"); return MARIE_ERR_BAD_ARG; }
   cudaStream_t s = (cudaStream_t)stream;
   const zd* b = (const zd*)b_;
   zd* x = (zd*)x_;
@@ -910,8 +920,17 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
     MARIE_TRY(gmres_core<double>(h, nrhs, V, m, x, bnorm, tolrel, o->maxit, all, log, &mv64, s, sc));
     MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, trel, &mv64, s, sc));
   } else {
+    const bool block = o->mode == MARIE_SOLVE_MIXED_BLOCK;
+    const int mb = o->block_steps > 0 ? o->block_steps : 20;
     cplx<float>* V = nullptr;
-    MARIE_TRY(sc.get(&V, (size_t)nrhs * (m + 1) * Nb));
+    cplx<float>* BW = nullptr;
+    if (!block) {
+      MARIE_TRY(sc.get(&V, (size_t)nrhs * (m + 1) * Nb));
+    } else {
+      // block basis (block_steps + 1) x nrhs vectors and the block W
+      MARIE_TRY(sc.get(&V, (size_t)(mb + 1) * nrhs * Nb));
+      MARIE_TRY(sc.get(&BW, (size_t)nrhs * Nb));
+    }
     std::vector<double> rel(nrhs, 1.0);
     if (o->x0_present) {
       MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, rel, &mv64, s, sc));
@@ -935,11 +954,6 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
       for (int r = 0; r < nrhs; ++r)
         if (rel[r] > o->tol && std::isfinite(rel[r]) && log[r].status == MARIE_OK) { todo[r] = 1; ++n; }
       if (n == 0) break;
-      unsigned char* d_todo = nullptr;
-      MARIE_TRY(sc.get(&d_todo, nrhs));
-      MARIE_TRY(chan_put(h, SLOT_TODO, nrhs, d_todo, todo.data(), nrhs, s));
-      k_convert<double, float><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)r64, Nb, V, (int64_t)(m + 1) * Nb, Nb, d_todo);
-      MARIE_LAUNCH_CHECK();
       // inner problem A d = r: relative tolerance w.r.t. ||r||, asking for just
       // enough reduction to reach the outer target (bounded by the c64 floor)
       std::vector<double> rn(nrhs), tin(nrhs);
@@ -948,7 +962,26 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
         tin[r] = std::min(0.5, std::max(floor_tol, safety * o->tol / std::max(rel[r], 1e-300)));
       }
       std::vector<RhsLog> ilog(nrhs);
-      MARIE_TRY(gmres_core<float>(h, nrhs, V, m, x, rn, tin, o->maxit, todo, ilog, &mv32, s, sc));
+      if (block) {
+        // the right-hand sides still above tol share one block Krylov space
+        std::vector<int> cols;
+        std::vector<double> cn, ct;
+        for (int r = 0; r < nrhs; ++r)
+          if (todo[r]) {
+            cols.push_back(r);
+            cn.push_back(rn[r]);
+            ct.push_back(tin[r] * rn[r]);
+          }
+        MARIE_TRY(bgmres_core(h, cols, r64, x, cn, ct, mb, o->maxit, V, BW, ilog, &mv32, s, sc));
+      } else {
+        unsigned char* d_todo = nullptr;
+        MARIE_TRY(sc.get(&d_todo, nrhs));
+        MARIE_TRY(chan_put(h, SLOT_TODO, nrhs, d_todo, todo.data(), nrhs, s));
+        k_convert<double, float><<<vgrid(Nb, nrhs), 256, 0, s>>>((const cplx<double>*)r64, Nb, V, (int64_t)(m + 1) * Nb,
+                                                                 Nb, d_todo);
+        MARIE_LAUNCH_CHECK();
+        MARIE_TRY(gmres_core<float>(h, nrhs, V, m, x, rn, tin, o->maxit, todo, ilog, &mv32, s, sc));
+      }
       for (int r = 0; r < nrhs; ++r) {
         if (!todo[r]) continue;
         log[r].iters += ilog[r].iters;
@@ -985,7 +1018,9 @@ extern "C" marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, v
   if (!h || !b_host || !x_host || !o) { set_error("NULL argument"); return MARIE_ERR_BAD_ARG; }
   if (nrhs < 1) { set_error("nrhs must be >= 1"); return MARIE_ERR_BAD_ARG; }
   const int64_t Nb = h->Nb;
-  int cs = o->mode == MARIE_SOLVE_MIXED ? h->p32.ws_rhs : (h->p64.built ? h->p64.ws_rhs : h->pff.ws_rhs);
+  // block mode: one chunk, so that all right-hand sides share the block space
+  int cs = o->mode == MARIE_SOLVE_MIXED_BLOCK ? (int)nrhs
+           : o->mode == MARIE_SOLVE_MIXED ? h->p32.ws_rhs : (h->p64.built ? h->p64.ws_rhs : h->pff.ws_rhs);
   // MARIE_HOST_CHUNK: right-hand sides per chunk of the host-buffer solve
   if (const char* e = getenv("MARIE_HOST_CHUNK")) {
     if (atoi(e) > 0) cs = atoi(e);

@@ -123,6 +123,10 @@ struct marie_vie {
   // engine behind the chunk copies of the host-buffer solve.
   unsigned char* hio = nullptr;
   size_t hio_cap = 0;
+  // the block solver's small matrices (pinned, device-mapped) and its cuBLAS handle
+  unsigned char* bio = nullptr;
+  size_t bio_cap = 0;
+  void* blas = nullptr;
   // CUDA graphs of Arnoldi windows (the launches between two host
   // synchronisations of the GMRES loop), keyed by every pointer and size the
   // launches capture; replayed by later cycles and solves of the same shape.
@@ -140,6 +144,7 @@ namespace marie {
 marie_status dev_alloc(marie_vie* h, void** p, size_t bytes);
 void dev_free_all(marie_vie* h);
 void graphs_free(marie_vie* h);
+void blas_free(marie_vie* h);
 
 enum OpKind { OP_N = 0, OP_N_ADJ = 1, OP_K = 2, OP_K_ADJ = 3 };
 

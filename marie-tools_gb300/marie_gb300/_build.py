@@ -83,7 +83,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         order = sorted(srcs, key=lambda it: (not it[1].startswith("fast"), it[1]))
         objs = list(ex.map(compile_one, order))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcublas"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

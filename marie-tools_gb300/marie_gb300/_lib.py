@@ -24,7 +24,7 @@ C128, C64 = 0, 1
 # float-float arithmetic (grid edges 16*NB, NB <= 8; exclusive with bit 1)
 PREC_C128, PREC_C64, PREC_C128FF = 1, 2, 4
 PWC, PWL = 0, 1
-SOLVE_FP64, SOLVE_MIXED = 0, 1
+SOLVE_FP64, SOLVE_MIXED, SOLVE_MIXED_BLOCK = 0, 1, 2
 
 
 class MarieError(RuntimeError):
@@ -50,7 +50,7 @@ class VieDesc(ct.Structure):
 class GmresOpts(ct.Structure):
     _fields_ = [("restart", ct.c_int32), ("maxit", ct.c_int32), ("tol", ct.c_double), ("mode", ct.c_int32),
                 ("x0_present", ct.c_int32), ("inner_tol", ct.c_double), ("max_refine", ct.c_int32),
-                ("inner_safety", ct.c_double), ("adjoint", ct.c_int32)]
+                ("inner_safety", ct.c_double), ("adjoint", ct.c_int32), ("block_steps", ct.c_int32)]
 
 
 class GmresReport(ct.Structure):

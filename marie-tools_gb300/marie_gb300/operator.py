@@ -13,7 +13,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import C128, C64, PWC, PWL, SOLVE_FP64, SOLVE_MIXED, check
+from ._lib import C128, C64, PWC, PWL, SOLVE_FP64, SOLVE_MIXED, SOLVE_MIXED_BLOCK, check
 
 
 def _dptr(a: np.ndarray):
@@ -276,11 +276,13 @@ class VieOperator:
 
     # -- solve ----------------------------------------------------------------
     def _run_gmres(self, fn, bptr, xptr, nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
-                   raise_on_fail, inner_safety=0.0, adjoint=False):
-        o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol,
-                           mode=SOLVE_MIXED if mode == "mixed" else SOLVE_FP64,
+                   raise_on_fail, inner_safety=0.0, adjoint=False, block_steps=0):
+        modes = {"fp64": SOLVE_FP64, "mixed": SOLVE_MIXED, "block": SOLVE_MIXED_BLOCK}
+        if mode not in modes:
+            raise ValueError(f"mode must be one of {sorted(modes)}")
+        o = _lib.GmresOpts(restart=restart, maxit=maxit, tol=tol, mode=modes[mode],
                            x0_present=1 if x0 else 0, inner_tol=inner_tol, max_refine=max_refine,
-                           inner_safety=inner_safety, adjoint=1 if adjoint else 0)
+                           inner_safety=inner_safety, adjoint=1 if adjoint else 0, block_steps=block_steps)
         it = np.zeros(nrhs, np.int32); ou = np.zeros(nrhs, np.int32); li = np.zeros(nrhs, np.int32)
         tr = np.zeros(nrhs, np.float64); st = np.zeros(nrhs, np.int32); rl = np.zeros(nrhs, np.int32)
         rv = np.zeros((nrhs, resvec_cap), np.float64)
@@ -294,9 +296,12 @@ class VieOperator:
                            rep.matvecs_c128, rep.matvecs_c64, ok=(s == 0))
 
     def gmres(self, b, x=None, *, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
-              max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0, adjoint=False):
+              max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0, adjoint=False, block_steps=0):
         """Batched is_gmres_vie (is_gmres_vie.m:1-30); b: (nrhs*N_b) complex128 CUDA.
-        adjoint=True solves A^H x = b."""
+        mode: "fp64" (the drop-in), "mixed" (complex64 GMRES per right-hand
+        side inside FP64 refinement) or "block" (the same refinement with one
+        block Krylov space for all right-hand sides, block_steps block
+        Arnoldi steps per cycle).  adjoint=True solves A^H x = b."""
         import torch
         b = b.contiguous()
         if b.dtype != torch.complex128 or b.device.type != "cuda":
@@ -307,11 +312,11 @@ class VieOperator:
             x = torch.zeros_like(b)
         report = self._run_gmres(self._lib.marie_gmres_vie, ct.c_void_p(b.data_ptr()), ct.c_void_p(x.data_ptr()),
                                  nrhs, x0, restart, tol, maxit, mode, inner_tol, max_refine, resvec_cap,
-                                 raise_on_fail, inner_safety, adjoint)
+                                 raise_on_fail, inner_safety, adjoint, block_steps)
         return x, report
 
     def gmres_host(self, b, x=None, *, out=None, restart=50, tol=1e-6, maxit=200, mode="fp64", inner_tol=1e-7,
-                   max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0):
+                   max_refine=10, resvec_cap=4096, raise_on_fail=False, inner_safety=0.0, block_steps=0):
         """is_gmres_vie on host buffers (marie_gmres_vie_host): b is a CPU
         complex128 tensor (nrhs*N_b), page-locked for copy/compute overlap.
         x (optional) holds x0 and receives the solution; otherwise the
@@ -327,7 +332,7 @@ class VieOperator:
             raise ValueError("x / out must match b")
         report = self._run_gmres(self._lib.marie_gmres_vie_host, ct.c_void_p(b.data_ptr()),
                                  ct.c_void_p(x.data_ptr()), nrhs, x0, restart, tol, maxit, mode, inner_tol,
-                                 max_refine, resvec_cap, raise_on_fail, inner_safety)
+                                 max_refine, resvec_cap, raise_on_fail, inner_safety, False, block_steps)
         return x, report
 
     # -- right-hand sides -----------------------------------------------------
