@@ -71,6 +71,11 @@ static void blas_mode_set(cublasHandle_t b) {
   if (m == "bf16x9") {
     cublasSetMathMode(b, CUBLAS_FP32_EMULATED_BF16X9_MATH);
     cublasSetEmulationStrategy(b, CUBLAS_EMULATION_STRATEGY_EAGER);
+    // no Inf/NaN propagation through the emulated products (it costs a scan
+    // of both operands per GEMM): the right-hand sides are checked finite on
+    // entry and every refinement step's FP64 residual, computed outside
+    // these GEMMs, catches a non-finite solution
+    cublasSetEmulationSpecialValuesSupport(b, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE);
   } else if (m == "tf32") {
     cublasSetMathMode(b, CUBLAS_TF32_TENSOR_OP_MATH);
   } else {
