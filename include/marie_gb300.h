@@ -150,7 +150,7 @@ typedef struct {
                              the FP64 true residual decides convergence either way */
   int32_t adjoint;        /* 1: solve A^H x = b (A^H as marie_vie_apply_adjoint), for adjoint
                              sensitivities; 0: A x = b */
-  int32_t block_steps;    /* MIXED_BLOCK: block Arnoldi steps per cycle (0 = 20); the block
+  int32_t block_steps;    /* MIXED_BLOCK: block Arnoldi steps per cycle (0 = 30); the block
                              basis holds (block_steps+1) x nrhs complex64 vectors */
 } marie_gmres_opts;
 

@@ -921,7 +921,9 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
     MARIE_TRY(true_residual(h, nrhs, b, x, r64, all, bnorm, trel, &mv64, s, sc));
   } else {
     const bool block = o->mode == MARIE_SOLVE_MIXED_BLOCK;
-    const int mb = o->block_steps > 0 ? o->block_steps : 20;
+    // 30 block steps per cycle: at 128^3 PWL with 64 loop ports 20 / 30 /
+    // 40 / 50 / 60 take 185 / 143 / 139 / 142 / 150 block steps, 30 the least time
+    const int mb = o->block_steps > 0 ? o->block_steps : 30;
     cplx<float>* V = nullptr;
     cplx<float>* BW = nullptr;
     if (!block) {

@@ -15,6 +15,8 @@
  *   Jout = marie_mex('mvp_N' | 'mvp_herm_adj_N' | 'mvp_K' | 'mvp_herm_adj_K', h, Jin)
  *   [x, iter, resvec] = marie_mex('gmres', h, b, restart, tol, maxit, x0 [, mode])
  *                                                   % is_gmres_vie.m:1; b may be N_b x nrhs
+ *       mode 0: FP64 (default), 1: complex64 GMRES per column + FP64 refinement,
+ *       2: the same refinement with one block Krylov space for all columns
  *   marie_mex('destroy', h)
  *   hp = marie_mex('svie_pfft_create', h, N_sie, pfft_PS, pfft_Z_cc, pfft_Z_bc_N, ext_Mc_inv [, M1, M2])
  *       h: handle on the pFFT grid (MREDM.operators.pfft_N); sparse complex operands as in
