@@ -607,12 +607,19 @@ def run_uneven(args):
                       "chosen": op.tiles()["width"]})
         insts.append((d, op, b))
     t_setup = time.time() - t0
-    kw = dict(restart=50, tol=1e-6, maxit=200, mode="mixed", inner_tol=1e-7)
+    kw = dict(restart=50, tol=1e-6, maxit=200, mode="mixed", inner_tol=1e-7, block_steps=BLOCK_STEPS)
     reps = {}
+
+    def mode_of(op, b):
+        # per-RHS mixed by default: the block solver's host synchronisations
+        # per block step (block QR, least squares) cost more than its fewer
+        # operator applications save on these small bodies (block GMRES for
+        # the multi-loop bodies: 12.5 against 18.0 solves/s on four streams)
+        return args.solver or "mixed"
 
     def solve(inst):
         d, op, b = inst
-        reps[d["i"]] = op.gmres(b, **kw)[1]
+        reps[d["i"]] = op.gmres(b, **dict(kw, mode=mode_of(op, b)))[1]
 
     for _ in range(max(1, args.warmup)):
         _concurrent(torch, insts, solve, args.streams)
@@ -637,7 +644,7 @@ def run_uneven(args):
 
     def solve_host(item):
         (op, b), x = item
-        op.gmres_host(b, out=x, **kw)
+        op.gmres_host(b, out=x, **dict(kw, mode=mode_of(op, b)))
 
     _concurrent(torch, hio, solve_host, args.streams)
     e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -663,7 +670,8 @@ def run_uneven(args):
         "config": {"workload": "16 PWC ellipsoid phantoms, edges from {48..128} at 2 mm, 128/297.2 MHz, 1-8 loops",
                    "loops_total": total, "restart": 50, "tol": 1e-6, "near_zone": args.near,
                    "schedule": f"bodies on {args.streams} concurrent CUDA streams (host threads), each body one "
-                               "batched solve of its loops; z-pass tiles from the library's autotuner"},
+                               "batched solve of its loops; z-pass tiles from the library's autotuner",
+                   "solver": args.solver or "mixed"},
         "e2e": {"value": round(total / (ms_e2e * 1e-3), 4), "unit": "solves/s",
                 "h2d_bytes_per_step": int(sum(b.numel() * 16 for _, b in hb)),
                 "d2h_bytes_per_step": int(sum(x.numel() * 16 for x in hx))},

@@ -68,7 +68,10 @@ static const char* blas_mode() {
 
 static void blas_mode_set(cublasHandle_t b) {
   const std::string m = blas_mode();
-  if (m == "bf16x9") {
+  if (m == "bf16x9s") {   // with Inf/NaN propagation
+    cublasSetMathMode(b, CUBLAS_FP32_EMULATED_BF16X9_MATH);
+    cublasSetEmulationStrategy(b, CUBLAS_EMULATION_STRATEGY_EAGER);
+  } else if (m == "bf16x9") {
     cublasSetMathMode(b, CUBLAS_FP32_EMULATED_BF16X9_MATH);
     cublasSetEmulationStrategy(b, CUBLAS_EMULATION_STRATEGY_EAGER);
     // no Inf/NaN propagation through the emulated products (it costs a scan
@@ -433,6 +436,9 @@ static marie_status bgmres_core(marie_vie* h, const std::vector<int>& cols, cons
     // x += V_{0:j} Y
     const int64_t n = (int64_t)(j + 1) * p;
     lsq.solve(j, Y);
+    // the upload area still feeds the last block QR's normalisation until
+    // the stream gets there
+    MARIE_CUDA_TRY(cudaStreamSynchronize(s));
     cplx<float>* up = reinterpret_cast<cplx<float>*>(h->bio + bio_up(p, mb));
     to_c64(Y, up);
     MARIE_TRY(bio_move(h, bio_up(p, mb), w.Sm, (size_t)n * p * 8, false, s));

@@ -104,3 +104,38 @@ def test_block_bad_args():
             op.gmres(b, mode="block", raise_on_fail=True, **kw)
         assert ei.value.status == 1
     op.close()
+
+
+@pytest.mark.gpu
+def test_block_solves_on_concurrent_streams():
+    """Two handles solving in block mode at once from two host threads, each
+    on its own stream (each handle's pinned staging area and GEMM handle are
+    its own): every solve converges and matches the same solve run alone."""
+    import threading
+    cases = [_case("pwl_4"), _case("pwc_5")]
+    rhs = [torch.from_numpy(_rhs(mv, 3, seed=5 + k).reshape(-1)).cuda() for k, (_, _, mv) in enumerate(cases)]
+    seq = [op.gmres(b, tol=1e-6, mode="block", block_steps=4)[0].cpu() for (op, _, _), b in zip(cases, rhs)]
+    out, errs = [None, None], []
+
+    def work(k):
+        try:
+            st = torch.cuda.Stream()
+            with torch.cuda.stream(st):
+                for _ in range(3):
+                    x, rep = cases[k][0].gmres(rhs[k], tol=1e-6, mode="block", block_steps=4)
+                    assert rep.ok
+                st.synchronize()
+                out[k] = x.cpu()
+        except Exception as e:
+            errs.append(e)
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errs, errs
+    for k in range(2):     # cuBLAS may pick other GEMM algorithms with several streams active
+        assert rel_err(out[k].numpy(), seq[k].numpy()) <= 1e-5, k
+    for op, _, _ in cases:
+        op.close()
