@@ -194,6 +194,19 @@ marie_status marie_gmres_vie_host(marie_vie* h, const void* b_host, void* x_host
  * of the adjoint gradient. */
 marie_status marie_vie_set_materials(marie_vie* h, const double* Mr_body);
 
+/* H (M x p complex64, column-major, leading dimension ldh) = V^H W for
+ * complex64 device arrays V (K x M, column a at V + a*ldv) and W (K x p,
+ * p <= 64), on the tensor cores (tcgen05, TF32 with three split products);
+ * the block GMRES solver's projection and Gram-matrix kernel.  ldv and ldw
+ * even, V and W 16-byte aligned; part: device scratch of
+ * marie_block_gemm_part_floats(K, M) floats; err: device int, set to 1 if a
+ * bounded device wait expired.  Enqueued on stream.  No counterpart in the
+ * reference (MATLAB's V'*W). */
+marie_status marie_block_gemm_cn(const void* V, int64_t ldv, const void* W, int64_t ldw, int64_t K, int32_t M,
+                                 int32_t p, void* H, int64_t ldh, void* part, int64_t part_floats, void* err,
+                                 void* stream);
+int64_t marie_block_gemm_part_floats(int64_t K, int32_t M);
+
 /* Frees the GMRES workspace the handle keeps between solves (Krylov basis,
  * residual vectors; reused by the next solve of the same or smaller shape).
  * No counterpart in the reference (MATLAB frees its arrays itself). */

@@ -23,7 +23,8 @@
 // The projections, updates, Gram matrices and combinations are GEMMs of a
 // tall (N_b rows) operand with (j+1)p or p columns: cuBLAS complex GEMMs on
 // the tensor cores (FP32 emulated by BF16x9 products, FP32 accumulation;
-// MARIE_BLOCK_GEMM=fp32 runs them on the FP32 pipe instead).  The small
+// MARIE_BLOCK_GEMM=fp32 runs them on the FP32 pipe instead;
+// MARIE_BLOCK_PROJ=tcgen05 runs the projections on bproj.cu's kernel).  The small
 // p x p and (j+2)p x p matrices move through pinned, device-mapped host
 // memory by a kernel (the status-channel discipline).
 #include <chrono>
@@ -245,16 +246,55 @@ struct BlockWork {
   cplx<float>* Gm = nullptr;   // p x p Gram matrix
   cplx<float>* Sm = nullptr;   // uploads: R^{-1}, Y, Z ((mb+1)p x p)
   int* map = nullptr;          // p rhs indices
-  cplx<float>* part = nullptr; // split-contraction partial products
+  cplx<float>* part = nullptr; // split-contraction partial products (cuBLAS path)
   int64_t part_cap = 0;
+  float* tpart = nullptr;      // partial sums of the tensor-core path
+  int64_t tpart_floats = 0;
+  bool tc = false;             // projections and Gram matrices on the tensor-core kernel
 };
 
-// Offsets in the pinned buffer
+// Offsets in the pinned buffer; the last 64 bytes hold the tensor-core
+// kernel's error word
 static size_t bio_need(int p, int mb) { return (size_t)(2 * mb * p * p + p * p + (mb + 1) * p * p) * 8 + 64; }
+static size_t bio_err(int p, int mb) { return bio_need(p, mb) - 64; }
 static size_t bio_h1(int, int) { return 0; }
 static size_t bio_h2(int p, int mb) { return (size_t)mb * p * p * 8; }
 static size_t bio_gm(int p, int mb) { return (size_t)2 * mb * p * p * 8; }
 static size_t bio_up(int p, int mb) { return (size_t)(2 * mb * p * p + p * p) * 8; }
+
+// MARIE_BLOCK_PROJ=tcgen05: the projections V^H W on this library's
+// tensor-core kernel (bproj.cu, TF32 with three split products) instead of
+// cuBLAS's emulated FP32.  Off by default: at 128^3 PWL with 64 ports it
+// ran no faster and its ~1e-6 relative error cost orthogonality (167 block
+// steps and three refinement steps against 143 and two).
+static bool proj_tcgen05() {
+  static const bool v = [] {
+    const char* e = getenv("MARIE_BLOCK_PROJ");
+    return e && std::string(e) == "tcgen05";
+  }();
+  return v;
+}
+
+// H (m x p, ld m) = A^H B for the N_b-row blocks A (m columns) and B (p columns)
+static marie_status proj_cn(marie_vie* h, BlockWork& w, cublasHandle_t bl, int64_t m, const cplx<float>* A,
+                            const cplx<float>* B, cplx<float>* H, cudaStream_t s) {
+  if (w.tc) {
+    unsigned char* qd = nullptr;
+    MARIE_CUDA_TRY(cudaHostGetDevicePointer((void**)&qd, h->bio, 0));
+    return block_gemm_cn(A, w.Nb, B, w.Nb, w.Nb, (int)m, w.p, H, m, w.tpart, w.tpart_floats,
+                         (int*)(qd + bio_err(w.p, w.mb)), s);
+  }
+  return cgemm_cn(bl, m, w.p, w.Nb, A, w.Nb, B, w.Nb, H, m, w.part, w.part_cap, s);
+}
+
+// after a synchronisation: did a tensor-core wait expire?
+static marie_status tc_check(marie_vie* h, const BlockWork& w) {
+  if (w.tc && *reinterpret_cast<volatile int*>(h->bio + bio_err(w.p, w.mb))) {
+    set_error("block GEMM: a bounded tensor-core wait expired");
+    return MARIE_ERR_DEVICE_TIMEOUT;
+  }
+  return MARIE_OK;
+}
 
 static void to_c64(const std::vector<zc>& a, cplx<float>* dst) {
   for (size_t i = 0; i < a.size(); ++i) dst[i] = cplx<float>{(float)a[i].real(), (float)a[i].imag()};
@@ -277,9 +317,13 @@ static marie_status block_qr(marie_vie* h, BlockWork& w, cublasHandle_t bl, cplx
   cplx<float>* b = dst;
   int passes = 2, shifts = 0;
   for (int pass = 0; pass < passes; ++pass) {
+    // the Gram matrix in cuBLAS's FP32-accurate products: the Cholesky
+    // factor needs its small eigenvalues (the tensor-core kernel's ~1e-6
+    // relative error is enough for the projections, not here)
     MARIE_TRY(cgemm_cn(bl, p, p, Nb, a, Nb, a, Nb, w.Gm, p, w.part, w.part_cap, s));
     MARIE_TRY(bio_move(h, bio_gm(p, w.mb), w.Gm, (size_t)p * p * 8, true, s));
     MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+    MARIE_TRY(tc_check(h, w));
     const cplx<float>* g = reinterpret_cast<const cplx<float>*>(hb + bio_gm(p, w.mb));
     std::vector<zc> G((size_t)p * p);
     double tr = 0;
@@ -352,12 +396,16 @@ static marie_status bgmres_core(marie_vie* h, const std::vector<int>& cols, cons
   MARIE_TRY(sc.get(&w.map, (size_t)p + 1));
   w.part_cap = (int64_t)65 * mb * p * p;
   MARIE_TRY(sc.get(&w.part, (size_t)w.part_cap));
+  w.tc = p <= 64 && Nb % 2 == 0 && proj_tcgen05();
+  w.tpart_floats = block_gemm_part_floats(Nb, mb * p);
+  if (w.tc) MARIE_TRY(sc.get(&w.tpart, (size_t)w.tpart_floats));
   MARIE_TRY(bio_reserve(h, bio_need(p, mb)));
   cublasHandle_t bl = nullptr;
   MARIE_TRY(blas_handle(h, s, &bl));
   const cuComplex one = {1.f, 0.f}, zero = {0.f, 0.f}, mone = {-1.f, 0.f};
   // rhs map and the residual block in complex64
   MARIE_CUDA_TRY(cudaStreamSynchronize(s));
+  *reinterpret_cast<volatile int*>(h->bio + bio_err(p, mb)) = 0;
   std::memcpy(h->bio + bio_up(p, mb), cols.data(), (size_t)p * sizeof(int));
   MARIE_TRY(bio_move(h, bio_up(p, mb), w.map, (size_t)((p + 1) / 2) * 8, false, s));
   k_gather_block<<<vgrid(Nb, p), 256, 0, s>>>(r64, Nb, w.W, Nb, w.map);
@@ -381,10 +429,10 @@ static marie_status bgmres_core(marie_vie* h, const std::vector<int>& cols, cons
       ++*matvecs;
       if (prof.on) cudaEventRecord(prof.ev[1], s);
       const int64_t M = (int64_t)(j + 1) * p;
-      MARIE_TRY(cgemm_cn(bl, M, p, Nb, w.V, Nb, w.W, Nb, w.H1, M, w.part, w.part_cap, s));
+      MARIE_TRY(proj_cn(h, w, bl, M, w.V, w.W, w.H1, s));
       MARIE_TRY(cgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, Nb, p, M, mone, w.V, Nb, w.H1, M, one, w.W, Nb));
       if (cgs_passes() > 1) {
-        MARIE_TRY(cgemm_cn(bl, M, p, Nb, w.V, Nb, w.W, Nb, w.H2, M, w.part, w.part_cap, s));
+        MARIE_TRY(proj_cn(h, w, bl, M, w.V, w.W, w.H2, s));
         MARIE_TRY(cgemm(bl, CUBLAS_OP_N, CUBLAS_OP_N, Nb, p, M, mone, w.V, Nb, w.H2, M, one, w.W, Nb));
       } else {
         MARIE_CUDA_TRY(cudaMemsetAsync(w.H2, 0, sizeof(cplx<float>) * (size_t)M * p, s));

@@ -146,6 +146,14 @@ void dev_free_all(marie_vie* h);
 void graphs_free(marie_vie* h);
 void blas_free(marie_vie* h);
 
+// H (M x p, ldh) = V^H W on the tensor cores (bproj.cu); p <= 64; part:
+// block_gemm_part_floats(K, M) floats of scratch; err: device-visible word
+// set to 1 if a bounded wait expired.
+marie_status block_gemm_cn(const cplx<float>* V, int64_t ldv, const cplx<float>* W, int64_t ldw, int64_t K, int M,
+                           int p, cplx<float>* H, int64_t ldh, float* part, int64_t part_floats, int* err,
+                           cudaStream_t s);
+int64_t block_gemm_part_floats(int64_t K, int M);
+
 enum OpKind { OP_N = 0, OP_N_ADJ = 1, OP_K = 2, OP_K_ADJ = 3 };
 
 // Enqueue one operator application on `stream`.

@@ -104,6 +104,9 @@ _PROTOS = {
     "marie_vie_autotune": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, ct.c_int32, ct.c_int32, c_int32_p, c_double_p,
                                       ct.c_int32, c_int32_p, _vp]),
     "marie_vie_release_workspace": (ct.c_int, [_vp]),
+    "marie_block_gemm_cn": (ct.c_int, [_vp, ct.c_int64, _vp, ct.c_int64, ct.c_int64, ct.c_int32, ct.c_int32, _vp,
+                                       ct.c_int64, _vp, ct.c_int64, _vp, _vp]),
+    "marie_block_gemm_part_floats": (ct.c_int64, [ct.c_int64, ct.c_int32]),
     "marie_vie_set_materials": (ct.c_int, [_vp, c_double_p]),
     "marie_vie_info": (ct.c_int, [_vp, ct.POINTER(ct.c_int64)]),
     "marie_vie_fields": (ct.c_int, [_vp, ct.c_int32, _vp, _vp, _vp, _vp, _vp, ct.c_int32, _vp]),

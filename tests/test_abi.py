@@ -174,3 +174,33 @@ def test_embedded_descriptor_reaches_the_device_step(lib):
             VieOperator(P.n, P.res, P.freq, P.dims["idx_solution"], P.Mr, N, K, pwl=False, precisions=2 | 4,
                         max_rhs=1)
         assert e.value.status == 6 and "CUDA device" in str(e.value)
+
+
+def test_ctypes_structs_match_header(tmp_path):
+    """The Python mirror's ctypes structures have the header's layout
+    (sizes and field offsets, compiled with the host C compiler)."""
+    import shutil
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    structs = {"marie_gmres_opts": _lib.GmresOpts, "marie_gmres_report": _lib.GmresReport,
+               "marie_vie_desc": _lib.VieDesc, "marie_tucker_block": _lib.TuckerBlock, "marie_csr": _lib.Csr,
+               "marie_svie_pfft_desc": _lib.SviePfftDesc}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "marie_gb300.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, field, val = line.split()
+        got[(name, field)] = int(val)
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == ct.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)

@@ -139,3 +139,55 @@ def test_block_solves_on_concurrent_streams():
         assert rel_err(out[k].numpy(), seq[k].numpy()) <= 1e-5, k
     for op, _, _ in cases:
         op.close()
+
+
+@pytest.mark.gpu
+def test_block_warm_start_and_not_converged():
+    """A warm start (x0 near the solution) needs fewer block steps than a cold
+    one and still meets tol by the oracle's residual; one short cycle per
+    refinement step and one refinement step end with MARIE_ERR_NOT_CONVERGED
+    per right-hand side, reported, not raised."""
+    op, A, mv = _case("pwl_4")
+    B = _rhs(mv, 2, seed=9)
+    bd = torch.from_numpy(B.reshape(-1)).cuda()
+    xc, repc = op.gmres(bd, tol=1e-6, mode="block", block_steps=8)
+    X = np.stack([O.is_gmres_vie(A, B[r], 50, 1e-12, 200, np.zeros(B.shape[1]))[0] for r in range(2)])
+    x0 = torch.from_numpy((0.999 * X).reshape(-1)).cuda()
+    xw, repw = op.gmres(bd, x=x0.clone(), tol=1e-6, mode="block", block_steps=8)
+    assert repc.ok and repw.ok
+    assert repw.matvecs_c64 < repc.matvecs_c64
+    Xw = xw.cpu().numpy().reshape(2, -1)
+    for r in range(2):
+        assert np.linalg.norm(B[r] - A(Xw[r])) / np.linalg.norm(B[r]) <= 1e-6
+    xn, repn = op.gmres(bd, tol=1e-10, maxit=1, max_refine=1, mode="block", block_steps=2)
+    assert not repn.ok and np.all(repn.status == 4)
+    assert np.all(repn.true_resid > 1e-10)
+    op.close()
+
+
+@pytest.mark.gpu
+def test_block_solve_with_tensor_core_projections(tmp_path):
+    """The block solver with its projections on the tcgen05 kernel
+    (MARIE_BLOCK_PROJ=tcgen05, read once per process: run in a child
+    process) reaches tol by the oracle's residual."""
+    import os
+    import subprocess
+    import sys
+    root = Path(__file__).resolve().parent.parent
+    script = tmp_path / "solve.py"
+    script.write_text(
+        "import sys, numpy as np, torch\n"
+        f"sys.path[:0] = [{str(root)!r}, {str(root / 'marie-tools_gb300')!r}, {str(root / 'tests')!r}]\n"
+        "from test_gpu_block_gmres import _case, _rhs\n"
+        "op, A, mv = _case('pwl_4')\n"
+        "B = _rhs(mv, 4, seed=1)\n"
+        "x, rep = op.gmres(torch.from_numpy(B.reshape(-1)).cuda(), tol=1e-6, mode='block', block_steps=6)\n"
+        "X = x.cpu().numpy().reshape(4, -1)\n"
+        "r = max(np.linalg.norm(B[k] - A(X[k])) / np.linalg.norm(B[k]) for k in range(4))\n"
+        "print('RESULT', int(rep.ok), r)\n")
+    env = dict(os.environ, MARIE_BLOCK_PROJ="tcgen05")
+    out = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, env=env, timeout=600,
+                         cwd=str(root / "tests"))
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = [l for l in out.stdout.splitlines() if l.startswith("RESULT")][-1].split()
+    assert int(line[1]) == 1 and float(line[2]) <= 1e-6, line
