@@ -56,6 +56,14 @@ __global__ void k_add_block(zd* __restrict__ x, int64_t xrs, const cplx<float>* 
     xr[i] = xr[i] + zd{(double)d[i].x, (double)d[i].y};
 }
 
+// *flag = 2 if any of the n values is not finite
+__global__ void k_check_finite(const float* __restrict__ v, int64_t n, int* flag) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(v[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) *(volatile int*)flag = 2;
+}
+
 // 8-byte words between device and pinned, device-mapped host memory
 __global__ void k_words(const unsigned long long* __restrict__ src, unsigned long long* __restrict__ dst, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -77,11 +85,9 @@ static void blas_mode_set(cublasHandle_t b) {
     cublasSetEmulationStrategy(b, CUBLAS_EMULATION_STRATEGY_EAGER);
     // no Inf/NaN propagation through the emulated products (it costs a scan
     // of both operands per GEMM): the right-hand sides are checked finite on
-    // entry and every refinement step's FP64 residual, computed outside
-    // these GEMMs, catches a non-finite solution
+    // entry and every operator output W is checked by k_check_finite before
+    // it enters a GEMM
     cublasSetEmulationSpecialValuesSupport(b, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE);
-  } else if (m == "tf32") {
-    cublasSetMathMode(b, CUBLAS_TF32_TENSOR_OP_MATH);
   } else {
     cublasSetMathMode(b, CUBLAS_PEDANTIC_MATH);
   }
@@ -287,9 +293,15 @@ static marie_status proj_cn(marie_vie* h, BlockWork& w, cublasHandle_t bl, int64
   return cgemm_cn(bl, m, w.p, w.Nb, A, w.Nb, B, w.Nb, H, m, w.part, w.part_cap, s);
 }
 
-// after a synchronisation: did a tensor-core wait expire?
+// after a synchronisation: the status word (1: a tensor-core wait expired,
+// 2: a non-finite operator output)
 static marie_status tc_check(marie_vie* h, const BlockWork& w) {
-  if (w.tc && *reinterpret_cast<volatile int*>(h->bio + bio_err(w.p, w.mb))) {
+  const int f = *reinterpret_cast<volatile int*>(h->bio + bio_err(w.p, w.mb));
+  if (f == 2) {
+    set_error("block GMRES: non-finite operator output");
+    return MARIE_ERR_NONFINITE;
+  }
+  if (f) {
     set_error("block GEMM: a bounded tensor-core wait expired");
     return MARIE_ERR_DEVICE_TIMEOUT;
   }
@@ -427,6 +439,14 @@ static marie_status bgmres_core(marie_vie* h, const std::vector<int>& cols, cons
       MARIE_TRY(launch_matvec<float>(h, sc.adjoint ? MV_VIE_ADJ : MV_VIE, sc.adjoint ? OP_N_ADJ : OP_N, Vj, Nb, w.W,
                                      Nb, p, nullptr, s));
       ++*matvecs;
+      {
+        unsigned char* qd = nullptr;
+        MARIE_CUDA_TRY(cudaHostGetDevicePointer((void**)&qd, h->bio, 0));
+        k_check_finite<<<vgrid(2 * (int64_t)p * Nb, 1).x, 256, 0, s>>>(reinterpret_cast<const float*>(w.W),
+                                                                       2 * (int64_t)p * Nb,
+                                                                       (int*)(qd + bio_err(p, mb)));
+        MARIE_LAUNCH_CHECK();
+      }
       if (prof.on) cudaEventRecord(prof.ev[1], s);
       const int64_t M = (int64_t)(j + 1) * p;
       MARIE_TRY(proj_cn(h, w, bl, M, w.V, w.W, w.H1, s));
