@@ -269,10 +269,10 @@ static size_t bio_gm(int p, int mb) { return (size_t)2 * mb * p * p * 8; }
 static size_t bio_up(int p, int mb) { return (size_t)(2 * mb * p * p + p * p) * 8; }
 
 // MARIE_BLOCK_PROJ=tcgen05: the projections V^H W on this library's
-// tensor-core kernel (bproj.cu, TF32 with three split products) instead of
-// cuBLAS's emulated FP32.  Off by default: at 128^3 PWL with 64 ports it
-// ran no faster and its ~1e-6 relative error cost orthogonality (167 block
-// steps and three refinement steps against 143 and two).
+// tensor-core kernel (bproj.cu, TF32 with three split products, FP32
+// accuracy) instead of cuBLAS's emulated FP32.  Off by default: at 128^3
+// PWL with 64 ports it reads V at 1.9 TB/s where cuBLAS's kernels are
+// faster (22.7 against 21.4 s per solve).
 static bool proj_tcgen05() {
   static const bool v = [] {
     const char* e = getenv("MARIE_BLOCK_PROJ");

@@ -16,14 +16,16 @@
 //
 // CTA: 256 threads, one slice of the contraction (complex rows [i0, i1)) x
 // up to 512 basis vectors (two accumulators of 256 tensor-memory columns).
-// Chunks of 16 complex rows: the threads convert the chunk held in
-// registers into the shared-memory operand tiles (8-row x 16-byte core
-// matrices, K-major, no swizzle), one thread issues the chunk's MMAs and
-// commits them to an mbarrier, and all threads load the next chunk into
-// registers while the tensor core works.  Each CTA writes its partial sums;
-// k_bproj_sum adds the slices in a fixed order.  Every wait is bounded: on
-// expiry the CTA sets the error word, waits (bounded) for its own MMAs,
-// frees its tensor memory and returns.
+// Chunks of 8 complex rows in two shared-memory stages: the threads convert
+// the chunk held in registers into one stage's operand tiles (8-row x
+// 16-byte core matrices, K-major, no swizzle) while the tensor core
+// multiplies the other stage; one thread issues a chunk's MMAs and commits
+// them to the stage's mbarrier, and all threads then load the next chunk
+// into registers.  Every 256 chunks the accumulators are added into the
+// CTA's FP32 partial sums and restarted (short accumulation chains in the
+// tensor core); k_bproj_sum adds the slices in a fixed order (FP64).  Every
+// wait is bounded: on expiry the CTA sets the error word, waits (bounded)
+// for its own MMAs, frees its tensor memory and returns.
 #include <cstdint>
 
 #include "internal.h"
@@ -31,11 +33,13 @@
 namespace marie {
 
 constexpr int kBpThreads = 256;
-constexpr int kBpChunk = 16;                    // complex rows per chunk (32 floats per operand row)
+constexpr int kBpChunk = 8;                     // complex rows per chunk (16 floats = 64 B per operand row)
 constexpr int kBpN = 512;                       // basis vectors per CTA
-constexpr int kBpA = 128 * 128;                 // bytes of one A tile (128 rows x 128 B)
-constexpr int kBpB = kBpN * 128;                // bytes of one B tile
-constexpr int kBpSmem = 2 * kBpA + 2 * kBpB;    // A_hi, A_lo, B_hi, B_lo
+constexpr int kBpA = 128 * 64;                  // bytes of one A tile (128 rows x 64 B)
+constexpr int kBpB = kBpN * 64;                 // bytes of one B tile
+constexpr int kBpStage = 2 * kBpA + 2 * kBpB;   // A_hi, A_lo, B_hi, B_lo
+constexpr int kBpSmem = 2 * kBpStage;           // two stages
+constexpr int kBpChain = 256;                   // chunks accumulated in tensor memory between flushes
 constexpr long long kBpWaitLimit = 1ll << 22;   // mbarrier polls before giving up
 
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
@@ -44,29 +48,31 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
   return r;
 }
 
-// hi / lo split of four values
+// hi / lo split of four values: hi = rna_tf32(x), lo = x - hi exactly in
+// FP32 (|lo| <= 2^-12 |x|; the tensor core reads its top 19 bits, so lo
+// carries x to within 2^-23 |x|)
 __device__ __forceinline__ void split4(float4 v, uint4& hi, uint4& lo) {
   hi.x = tf32_rna(v.x);
   hi.y = tf32_rna(v.y);
   hi.z = tf32_rna(v.z);
   hi.w = tf32_rna(v.w);
-  lo.x = tf32_rna(v.x - __uint_as_float(hi.x));
-  lo.y = tf32_rna(v.y - __uint_as_float(hi.y));
-  lo.z = tf32_rna(v.z - __uint_as_float(hi.z));
-  lo.w = tf32_rna(v.w - __uint_as_float(hi.w));
+  lo.x = __float_as_uint(v.x - __uint_as_float(hi.x));
+  lo.y = __float_as_uint(v.y - __uint_as_float(hi.y));
+  lo.z = __float_as_uint(v.z - __uint_as_float(hi.z));
+  lo.w = __float_as_uint(v.w - __uint_as_float(hi.w));
 }
 
 // byte offset of (row, 16-byte column kq) in a K-major core-matrix tile with
-// 8 core matrices along K (128 bytes of K per row)
+// 4 core matrices along K (64 bytes of K per row)
 __device__ __forceinline__ uint32_t core_off(int row, int kq) {
-  return (uint32_t)((((row >> 3) << 3) + kq) << 7) + (uint32_t)((row & 7) << 4);
+  return (uint32_t)((((row >> 3) << 2) + kq) << 7) + (uint32_t)((row & 7) << 4);
 }
 
 // shared-memory matrix descriptor: K-major, no swizzle; core matrices 128 B
-// apart along K (leading byte offset) and 1024 B apart along M/N (stride byte
+// apart along K (leading byte offset) and 512 B apart along M/N (stride byte
 // offset); descriptor version 1 (sm_100 family)
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(512 >> 4) << 32) |
          (1ull << 46);
 }
 
@@ -110,7 +116,7 @@ struct BprojArgs {
 
 __global__ void __launch_bounds__(kBpThreads, 1) k_bproj(BprojArgs g) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) unsigned long long bar;
+  __shared__ __align__(8) unsigned long long bars[2];
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int slice = blockIdx.x, tile = blockIdx.y;
@@ -120,9 +126,8 @@ __global__ void __launch_bounds__(kBpThreads, 1) k_bproj(BprojArgs g) {
   const int nvalid = min(kBpN, g.M - a0);
   const int nB = (nvalid + 15) & ~15;                 // MMA N (multiple of 16)
   const uint32_t ncols = nB <= 32 ? 32 : nB <= 64 ? 64 : nB <= 128 ? 128 : nB <= 256 ? 256 : 512;
-  const uint32_t sA_hi = (uint32_t)__cvta_generic_to_shared(sm);
-  const uint32_t sA_lo = sA_hi + kBpA, sB_hi = sA_hi + 2 * kBpA, sB_lo = sB_hi + kBpB;
-  const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+  const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(sm);
+  const uint32_t sbar0 = (uint32_t)__cvta_generic_to_shared(&bars[0]);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      (uint32_t)__cvta_generic_to_shared(&tmem_slot)),
@@ -131,7 +136,8 @@ __global__ void __launch_bounds__(kBpThreads, 1) k_bproj(BprojArgs g) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar0 + 8) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -140,127 +146,107 @@ __global__ void __launch_bounds__(kBpThreads, 1) k_bproj(BprojArgs g) {
   const uint32_t tmem = tmem_slot;
 
   const int64_t nch = (i1 - i0 + kBpChunk - 1) / kBpChunk;
-  // per-thread float4 loads of a chunk: B rows q = tid + 256 u (u < 16),
-  // A (W) rows q = tid + 256 u (u < 2); q -> row = (q >> 6) * 8 + (q & 7),
-  // kq = (q >> 3) & 7, so the 8 threads of a quarter warp store 8 rows of one
-  // core-matrix column (distinct banks)
-  float4 rb[16], ra[2];
-  auto load = [&](int64_t ch) {
+  // per-thread float4 loads of a chunk: B rows q = tid + 256 u (u < 8), A (W)
+  // rows q = tid; q -> row = (q >> 5) * 8 + (q & 7), kq = (q >> 3) & 3, so
+  // the 8 threads of a quarter warp store 8 rows of one core-matrix column
+  // (distinct banks) and a warp reads 8 rows x 64 contiguous bytes
+  // three register sets: chunks ch+1 and ch+2 are in flight while chunk ch
+  // is converted (one CTA per SM: the loads in flight set the bandwidth)
+  float4 rb0[8], rb1[8], rb2[8], ra0, ra1, ra2;
+  // the thread's rows: base pointers at the slice start (row and column
+  // fixed for the whole slice), advanced by 16 floats per chunk
+  const float* bp[8];
+  unsigned bvalid = 0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int q = tid + kBpThreads * u;
+    const int row = ((q >> 5) << 3) + (q & 7), kq = (q >> 3) & 3;
+    if (row < nvalid) bvalid |= 1u << u;
+    bp[u] = g.V + 2 * ((int64_t)(a0 + (row < nvalid ? row : 0)) * g.ldv + i0) + 4 * kq;
+  }
+  const int ac = ((tid >> 5) << 3) + (tid & 7), akq = (tid >> 3) & 3;
+  const bool avalid = ac < g.p;
+  const float* ap = g.W + 2 * ((int64_t)(avalid ? ac : 0) * g.ldw + i0) + 4 * akq;
+  const int64_t nfull = (i1 - i0) / kBpChunk;         // chunks without a ragged end
+  auto load = [&](int64_t ch, float4 (&rb)[8], float4& ra) {
+    const int64_t off = ch * 2 * kBpChunk;
+    if (ch < nfull) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        rb[u] = (bvalid >> u) & 1u ? __ldg(reinterpret_cast<const float4*>(bp[u] + off))
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+      ra = avalid ? __ldg(reinterpret_cast<const float4*>(ap + off)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      return;
+    }
+    // the ragged last chunk: complex rows i and i + 1 of each float4 checked
     const int64_t ib = i0 + ch * kBpChunk;
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const int q = tid + kBpThreads * u;
-      const int row = ((q >> 6) << 3) + (q & 7), kq = (q >> 3) & 7;
+      const int kq = (q >> 3) & 3;
       const int64_t i = ib + 2 * kq;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row < nvalid && i < i1) {
-        const float* src = g.V + 2 * ((int64_t)(a0 + row) * g.ldv + i);
+      if (((bvalid >> u) & 1u) && i < i1) {
         if (i + 1 < i1) {
-          v = __ldg(reinterpret_cast<const float4*>(src));
+          v = __ldg(reinterpret_cast<const float4*>(bp[u] + off));
         } else {
-          const float2 h = __ldg(reinterpret_cast<const float2*>(src));
+          const float2 h = __ldg(reinterpret_cast<const float2*>(bp[u] + off));
           v = make_float4(h.x, h.y, 0.f, 0.f);
         }
       }
       rb[u] = v;
     }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int q = tid + kBpThreads * u;
-      const int c = ((q >> 6) << 3) + (q & 7), kq = (q >> 3) & 7;
-      const int64_t i = ib + 2 * kq;
+    {
+      const int64_t i = ib + 2 * akq;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (c < g.p && i < i1) {
-        const float* src = g.W + 2 * ((int64_t)c * g.ldw + i);
+      if (avalid && i < i1) {
         if (i + 1 < i1) {
-          v = __ldg(reinterpret_cast<const float4*>(src));
+          v = __ldg(reinterpret_cast<const float4*>(ap + off));
         } else {
-          const float2 h = __ldg(reinterpret_cast<const float2*>(src));
+          const float2 h = __ldg(reinterpret_cast<const float2*>(ap + off));
           v = make_float4(h.x, h.y, 0.f, 0.f);
         }
       }
-      ra[u] = v;
+      ra = v;
     }
   };
-  auto store = [&]() {
+  auto store = [&](int st, const float4 (&rb)[8], const float4& ra) {
+    unsigned char* base = sm + st * kBpStage;
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const int q = tid + kBpThreads * u;
-      const int row = ((q >> 6) << 3) + (q & 7), kq = (q >> 3) & 7;
+      const int row = ((q >> 5) << 3) + (q & 7), kq = (q >> 3) & 3;
       if (row < nB) {
         uint4 hi, lo;
         split4(rb[u], hi, lo);
         const uint32_t off = core_off(row, kq);
-        *reinterpret_cast<uint4*>(sm + 2 * kBpA + off) = hi;
-        *reinterpret_cast<uint4*>(sm + 2 * kBpA + kBpB + off) = lo;
+        *reinterpret_cast<uint4*>(base + 2 * kBpA + off) = hi;
+        *reinterpret_cast<uint4*>(base + 2 * kBpA + kBpB + off) = lo;
       }
     }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int q = tid + kBpThreads * u;
-      const int c = ((q >> 6) << 3) + (q & 7), kq = (q >> 3) & 7;
-      const float4 w = ra[u];
-      const float4 w2 = make_float4(w.y, -w.x, w.w, -w.z);   // (wi, -wr) of the two complex rows
+    {
+      const int c = ((tid >> 5) << 3) + (tid & 7), kq = (tid >> 3) & 3;
+      const float4 w2 = make_float4(ra.y, -ra.x, ra.w, -ra.z);   // (wi, -wr) of the two complex rows
       uint4 hi, lo;
-      split4(w, hi, lo);
+      split4(ra, hi, lo);
       uint32_t off = core_off(c, kq);
-      *reinterpret_cast<uint4*>(sm + off) = hi;
-      *reinterpret_cast<uint4*>(sm + kBpA + off) = lo;
+      *reinterpret_cast<uint4*>(base + off) = hi;
+      *reinterpret_cast<uint4*>(base + kBpA + off) = lo;
       split4(w2, hi, lo);
       off = core_off(64 + c, kq);
-      *reinterpret_cast<uint4*>(sm + off) = hi;
-      *reinterpret_cast<uint4*>(sm + kBpA + off) = lo;
+      *reinterpret_cast<uint4*>(base + off) = hi;
+      *reinterpret_cast<uint4*>(base + kBpA + off) = lo;
     }
   };
-
-  bool ok = true;
-  int64_t last = -1;                                  // last committed chunk
-  if (nch > 0) load(0);
-  for (int64_t ch = 0; ch < nch && ok; ++ch) {
-    if (ch > 0 && !mbar_wait(sbar, (uint32_t)((ch - 1) & 1))) {
-      ok = false;
-      break;
-    }
-    store();
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int n0 = min(nB, 256), n1 = nB - n0;
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {         // four K steps of 8 values (two core matrices)
-#pragma unroll
-        for (int t = 0; t < 3; ++t) {       // hi.hi, hi.lo, lo.hi
-          const uint64_t ad = smem_desc((t == 2 ? sA_lo : sA_hi) + s * 256);
-          const uint32_t bb = (t == 1 ? sB_lo : sB_hi) + s * 256;
-          const uint32_t acc = (ch > 0 || s > 0 || t > 0) ? 1u : 0u;
-          mma_tf32(tmem, ad, smem_desc(bb), idesc_tf32(n0), acc);
-          if (n1 > 0) mma_tf32(tmem + 256, ad, smem_desc(bb + 32 * 1024), idesc_tf32(n1), acc);
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(sbar)
-                   : "memory");
-    }
-    last = ch;
-    if (ch + 1 < nch) load(ch + 1);
-  }
-  // the last committed chunk's products (after an expired wait: one more
-  // bounded wait for what is in flight)
-  if (!ok) *(volatile int*)g.err = 1;
-  if (last >= 0) {
-    const bool done = mbar_wait(sbar, (uint32_t)(last & 1));
-    if (!done) *(volatile int*)g.err = 1;
-    ok = ok && done;
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
-    // epilogue: warp w reads lanes 32 (w & 3) .. +31, columns of its half
-    const int lane_base = (warp & 3) * 32;
-    const int m = lane_base + (tid & 31);
-    const int half = (nB + 63) / 64 * 32;           // columns per warp half, multiple of 32
-    const int c0 = (warp >> 2) * half, c1 = min(nB, c0 + half);
-    float* dst = g.part + ((int64_t)slice * g.Mpad + a0) * 128 + m;
-    for (int cb = c0; cb < c1; cb += 32) {
+  // tensor memory -> partial sums (the CTA's own rows of part): the first
+  // flush stores, later ones add in FP32
+  const int lane_base = (warp & 3) * 32;
+  const int m = lane_base + (tid & 31);
+  const int half = (nB + 63) / 64 * 32;               // columns per warp half, multiple of 32
+  const int fc0 = (warp >> 2) * half, fc1 = min(nB, fc0 + half);
+  float* dst = g.part + ((int64_t)slice * g.Mpad + a0) * 128 + m;
+  auto flush = [&](bool first) {
+    for (int cb = fc0; cb < fc1; cb += 32) {
       uint32_t r[32];
       const uint32_t taddr = tmem + ((uint32_t)lane_base << 16) + (uint32_t)cb;
       asm volatile(
@@ -274,8 +260,74 @@ __global__ void __launch_bounds__(kBpThreads, 1) k_bproj(BprojArgs g) {
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
       for (int j = 0; j < 32; ++j)
-        if (cb + j < c1) dst[(int64_t)(cb + j) * 128] = __uint_as_float(r[j]);
+        if (cb + j < fc1) {
+          float* q = dst + (int64_t)(cb + j) * 128;
+          *q = first ? __uint_as_float(r[j]) : *q + __uint_as_float(r[j]);
+        }
     }
+  };
+
+  bool ok = true;
+  int64_t last = -1;                                  // last committed chunk
+  int64_t chain0 = 0;                                 // first chunk of the current accumulation chain
+  // one chunk: convert it into its stage, multiply, refill its register set
+  // with chunk ch + 3, and at the end of a chain move the sums out; false
+  // after an expired wait (the same for every thread)
+  auto step = [&](int64_t ch, float4 (&rb)[8], float4& ra) -> bool {
+    const int st = (int)(ch & 1);
+    // the stage's previous chunk (ch - 2) must be multiplied before it is
+    // overwritten; the barrier makes an expired wait everyone's decision
+    const bool ready = ch < 2 || mbar_wait(sbar0 + 8 * st, (uint32_t)(((ch - 2) >> 1) & 1));
+    if (ready) store(st, rb, ra);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (!__syncthreads_and(ready)) return false;
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sA_hi = s0 + st * kBpStage, sA_lo = sA_hi + kBpA;
+      const uint32_t sB_hi = sA_hi + 2 * kBpA, sB_lo = sB_hi + kBpB;
+      const int n0 = min(nB, 256), n1 = nB - n0;
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {         // two K steps of 8 values (two core matrices)
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {       // hi.hi, hi.lo, lo.hi
+          const uint64_t ad = smem_desc((t == 2 ? sA_lo : sA_hi) + s * 256);
+          const uint32_t bb = (t == 1 ? sB_lo : sB_hi) + s * 256;
+          const uint32_t acc = (ch > chain0 || s > 0 || t > 0) ? 1u : 0u;
+          mma_tf32(tmem, ad, smem_desc(bb), idesc_tf32(n0), acc);
+          if (n1 > 0) mma_tf32(tmem + 256, ad, smem_desc(bb + 32 * 512), idesc_tf32(n1), acc);
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       sbar0 + 8 * st)
+                   : "memory");
+    }
+    last = ch;
+    if (ch + 3 < nch) load(ch + 3, rb, ra);
+    if (ch + 1 == nch || ch + 1 - chain0 == kBpChain) {
+      // end of an accumulation chain: wait for its products, move them out
+      const bool done = mbar_wait(sbar0 + 8 * st, (uint32_t)((ch >> 1) & 1));
+      if (!__syncthreads_and(done)) return false;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      flush(chain0 == 0);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      chain0 = ch + 1;
+    }
+    return true;
+  };
+  if (nch > 0) load(0, rb0, ra0);
+  if (nch > 1) load(1, rb1, ra1);
+  if (nch > 2) load(2, rb2, ra2);
+  for (int64_t ch = 0; ch < nch && ok; ch += 3) {
+    ok = step(ch, rb0, ra0);
+    if (ok && ch + 1 < nch) ok = step(ch + 1, rb1, ra1);
+    if (ok && ch + 2 < nch) ok = step(ch + 2, rb2, ra2);
+  }
+  if (!ok) {
+    // an expired wait: one more bounded wait for the products in flight
+    *(volatile int*)g.err = 1;
+    if (last >= 0 && !mbar_wait(sbar0 + 8 * (int)(last & 1), (uint32_t)((last >> 1) & 1)))
+      *(volatile int*)g.err = 1;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
