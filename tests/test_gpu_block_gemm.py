@@ -2,9 +2,10 @@
 tcgen05 kind::tf32 with three split products) against a complex128 product
 of the same complex64 data.
 
-Tolerance: every entry within 2e-6 of ||V_a|| ||W_c|| (the Cauchy-Schwarz
-bound of the entry): the split products carry ~2^-22 of each product and
-the sums are FP32 in the tensor core, then FP64 across contraction slices.
+Tolerance: every entry within 2e-7 of ||V_a|| ||W_c|| (the Cauchy-Schwarz
+bound of the entry; measured ~5.5e-8, FP32 level): the split products carry
+~2^-23 of each product, the tensor core sums chains of 256 chunks in FP32,
+the chains and the contraction slices are added in FP32 / FP64.
 Cases: one and several 512-column tiles, ragged column counts (1, 17, 300,
 1100), p = 1 / 7 / 64, an odd number of complex rows, leading dimensions
 larger than the row count, and misaligned arguments refused.
@@ -47,7 +48,7 @@ def test_block_gemm_matches_complex128(K, M, p, pad):
     ref = Vm.conj() @ Wm.T                                       # (M, p) = V^H W
     bound = torch.linalg.norm(Vm, dim=1)[:, None] * torch.linalg.norm(Wm, dim=1)[None, :]
     rel = ((H.to(torch.complex128) - ref).abs() / bound).max().item()
-    assert rel <= 2e-6, rel
+    assert rel <= 2e-7, rel
 
 
 @pytest.mark.gpu
@@ -61,7 +62,7 @@ def test_block_gemm_gram_and_bad_args():
     st, G, err = _gemm(W, W, K, p, p, K, K)
     assert st == 0 and err == 0
     Gd = G.to(torch.complex128)
-    assert (Gd - Gd.conj().T).abs().max().item() <= 2e-6 * Gd.diagonal().real.max().item()
+    assert (Gd - Gd.conj().T).abs().max().item() <= 2e-7 * Gd.diagonal().real.max().item()
     assert torch.linalg.eigvalsh(0.5 * (Gd + Gd.conj().T)).min().item() > 0
     st, _, _ = _gemm(W, W, K, p, 65, K, K)
     assert st == 1
