@@ -526,6 +526,57 @@ def run_matvec_only(args, wl):
     op.close()
 
 
+def run_block_gemm(args):
+    """The block solver's tensor-core projection H = V^H W (marie_block_gemm_cn)
+    on seeded complex64 data of the solver's shape: N_b rows, M basis
+    vectors, 64 right-hand sides; CUDA-event time over 5 calls after 3, bytes
+    read (V once, W once per 512-column tile) and the error against a
+    complex128 product (per entry, relative to ||V_a|| ||W_c||)."""
+    import ctypes as ct
+    import torch
+    import __graft_entry__ as ge
+    from marie_gb300 import _lib
+    ge.build()
+    lib = _lib.load()
+    K, M, p = args.block_gemm_rows, args.block_gemm, 64
+    g = torch.Generator(device="cuda").manual_seed(0)
+    V = torch.randn(M * K, dtype=torch.complex64, device="cuda", generator=g)
+    W = torch.randn(p * K, dtype=torch.complex64, device="cuda", generator=g)
+    H = torch.zeros(M * p, dtype=torch.complex64, device="cuda")
+    nf = lib.marie_block_gemm_part_floats(K, M)
+    part = torch.empty(nf, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    stream = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def call():
+        st = lib.marie_block_gemm_cn(ct.c_void_p(V.data_ptr()), K, ct.c_void_p(W.data_ptr()), K, K, M, p,
+                                     ct.c_void_p(H.data_ptr()), M, ct.c_void_p(part.data_ptr()), nf,
+                                     ct.c_void_p(err.data_ptr()), stream)
+        _lib.check(st)
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 5
+    Vm, Wm = V.reshape(M, K), W.reshape(p, K)
+    ref = torch.zeros(M, p, dtype=torch.complex128, device="cuda")
+    for k0 in range(0, K, 1 << 18):
+        ref += Vm[:, k0:k0 + (1 << 18)].to(torch.complex128).conj() @ Wm[:, k0:k0 + (1 << 18)].to(torch.complex128).T
+    bound = (torch.linalg.norm(Vm.to(torch.complex128), dim=1)[:, None] *
+             torch.linalg.norm(Wm.to(torch.complex128), dim=1)[None, :])
+    rel = ((H.reshape(p, M).T.to(torch.complex128) - ref).abs() / bound).max().item()
+    nbytes = (M + p * ((M + 511) // 512)) * K * 8
+    print(json.dumps({"block_gemm": {"rows": K, "basis_vectors": M, "rhs": p}, "ms": round(ms, 4),
+                      "bytes": nbytes, "achieved_GBs": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                      "rel_err_max": rel, "wait_expired": int(err.item())}), flush=True)
+
+
 def uneven_instances(seed=44, count=16, res=2e-3):
     """The uneven-size batch: `count` seeded PWC phantoms with grid edges drawn
     from {48, ..., 128} at 2 mm, 128 or 297.2 MHz, 1-8 loops on a ring around
@@ -696,6 +747,10 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     ap.add_argument("--streams", type=int, default=4, help="uneven16: concurrent CUDA streams for the bodies")
+    ap.add_argument("--block-gemm", type=int, default=0, metavar="M",
+                    help="profiling aid: the block solver's tensor-core projection V^H W (M basis vectors, "
+                         "--block-gemm-rows rows, 64 right-hand sides) on seeded data, timed")
+    ap.add_argument("--block-gemm-rows", type=int, default=2939712)
     ap.add_argument("--matvec-only", type=int, default=0,
                     help="profiling aid: build the workload, apply mvp_vie this many times, print per-pass times")
     ap.add_argument("--near", default="relative", choices=["standin", "relative"],
@@ -720,6 +775,9 @@ def main():
     wl["near"] = args.near
     if args.nrhs:
         wl["nrhs"] = args.nrhs
+    if args.block_gemm:
+        run_block_gemm(args)
+        return
     if args.matvec_only:
         run_matvec_only(args, wl)
         return
