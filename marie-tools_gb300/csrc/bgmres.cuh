@@ -384,33 +384,40 @@ static marie_status block_qr(marie_vie* h, BlockWork& w, cublasHandle_t bl, cplx
   return MARIE_OK;
 }
 
-// Inner block solve of one refinement step: A D = R for the p right-hand
-// sides cols[c] of r64 (FP64), D added to x.  V ((mb+1) p vectors) and Wb
-// (p vectors): complex64 device buffers.  tolabs[c]: absolute residual
-// target of column c; log[cols[c]] receives the residual history relative to
-// rnorm[c] (first entry 1), iterations and cycles.
-static marie_status bgmres_core(marie_vie* h, const std::vector<int>& cols, const zd* r64, zd* x,
-                                const std::vector<double>& rnorm, const std::vector<double>& tolabs, int mb,
-                                int maxcyc, cplx<float>* V, cplx<float>* Wb, std::vector<RhsLog>& log, int* matvecs,
-                                cudaStream_t s, Scratch& sc) {
-  const int p = (int)cols.size();
+// The block solver's device workspace for up to pmax right-hand sides and mb
+// block steps, from the solve's pool; allocated once per solve and shared by
+// its refinement steps.
+static marie_status block_work_alloc(marie_vie* h, BlockWork& w, int pmax, int mb, Scratch& sc) {
   const int64_t Nb = h->Nb;
-  BlockWork w;
-  w.p = p;
   w.mb = mb;
   w.Nb = Nb;
-  w.V = V;
-  w.W = Wb;
-  MARIE_TRY(sc.get(&w.H1, (size_t)mb * p * p));
-  MARIE_TRY(sc.get(&w.H2, (size_t)mb * p * p));
-  MARIE_TRY(sc.get(&w.Gm, (size_t)p * p));
-  MARIE_TRY(sc.get(&w.Sm, (size_t)(mb + 1) * p * p));
-  MARIE_TRY(sc.get(&w.map, (size_t)p + 1));
-  w.part_cap = (int64_t)65 * mb * p * p;
+  MARIE_TRY(sc.get(&w.V, (size_t)(mb + 1) * pmax * Nb));
+  MARIE_TRY(sc.get(&w.W, (size_t)pmax * Nb));
+  MARIE_TRY(sc.get(&w.H1, (size_t)mb * pmax * pmax));
+  MARIE_TRY(sc.get(&w.H2, (size_t)mb * pmax * pmax));
+  MARIE_TRY(sc.get(&w.Gm, (size_t)pmax * pmax));
+  MARIE_TRY(sc.get(&w.Sm, (size_t)(mb + 1) * pmax * pmax));
+  MARIE_TRY(sc.get(&w.map, (size_t)pmax + 1));
+  w.part_cap = (int64_t)65 * mb * pmax * pmax;
   MARIE_TRY(sc.get(&w.part, (size_t)w.part_cap));
-  w.tc = p <= 64 && Nb % 2 == 0 && proj_tcgen05();
-  w.tpart_floats = block_gemm_part_floats(Nb, mb * p);
-  if (w.tc) MARIE_TRY(sc.get(&w.tpart, (size_t)w.tpart_floats));
+  w.tpart_floats = block_gemm_part_floats(Nb, mb * std::min(pmax, 64));
+  if (pmax <= 64 && Nb % 2 == 0 && proj_tcgen05()) MARIE_TRY(sc.get(&w.tpart, (size_t)w.tpart_floats));
+  return MARIE_OK;
+}
+
+// Inner block solve of one refinement step: A D = R for the p right-hand
+// sides cols[c] of r64 (FP64), D added to x; w from block_work_alloc with
+// pmax >= p.  tolabs[c]: absolute residual target of column c;
+// log[cols[c]] receives the residual history relative to rnorm[c] (first
+// entry 1), iterations and cycles.
+static marie_status bgmres_core(marie_vie* h, const std::vector<int>& cols, const zd* r64, zd* x,
+                                const std::vector<double>& rnorm, const std::vector<double>& tolabs, int maxcyc,
+                                BlockWork& w, std::vector<RhsLog>& log, int* matvecs, cudaStream_t s, Scratch& sc) {
+  const int p = (int)cols.size();
+  const int64_t Nb = h->Nb;
+  const int mb = w.mb;
+  w.p = p;
+  w.tc = p <= 64 && Nb % 2 == 0 && w.tpart != nullptr;
   MARIE_TRY(bio_reserve(h, bio_need(p, mb)));
   cublasHandle_t bl = nullptr;
   MARIE_TRY(blas_handle(h, s, &bl));

@@ -925,13 +925,13 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
     // 40 / 50 / 60 take 185 / 143 / 139 / 142 / 150 block steps, 30 the least time
     const int mb = o->block_steps > 0 ? o->block_steps : 30;
     cplx<float>* V = nullptr;
-    cplx<float>* BW = nullptr;
+    BlockWork bw;
     if (!block) {
       MARIE_TRY(sc.get(&V, (size_t)nrhs * (m + 1) * Nb));
     } else {
-      // block basis (block_steps + 1) x nrhs vectors and the block W
-      MARIE_TRY(sc.get(&V, (size_t)(mb + 1) * nrhs * Nb));
-      MARIE_TRY(sc.get(&BW, (size_t)nrhs * Nb));
+      // block basis (block_steps + 1) x nrhs vectors, the block W and the
+      // small matrices, shared by the refinement steps
+      MARIE_TRY(block_work_alloc(h, bw, nrhs, mb, sc));
     }
     std::vector<double> rel(nrhs, 1.0);
     if (o->x0_present) {
@@ -974,7 +974,7 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
             cn.push_back(rn[r]);
             ct.push_back(tin[r] * rn[r]);
           }
-        MARIE_TRY(bgmres_core(h, cols, r64, x, cn, ct, mb, o->maxit, V, BW, ilog, &mv32, s, sc));
+        MARIE_TRY(bgmres_core(h, cols, r64, x, cn, ct, o->maxit, bw, ilog, &mv32, s, sc));
       } else {
         unsigned char* d_todo = nullptr;
         MARIE_TRY(sc.get(&d_todo, nrhs));
