@@ -191,3 +191,20 @@ def test_block_solve_with_tensor_core_projections(tmp_path):
     assert out.returncode == 0, out.stderr[-2000:]
     line = [l for l in out.stdout.splitlines() if l.startswith("RESULT")][-1].split()
     assert int(line[1]) == 1 and float(line[2]) <= 1e-6, line
+
+
+@pytest.mark.gpu
+def test_block_solve_more_than_64_rhs():
+    """70 right-hand sides in one block (above the tensor-core kernel's 64:
+    the cuBLAS path for every GEMM), two block steps per cycle."""
+    op, A, mv = _case("pwl_4", max_rhs=70)
+    n = mv["b"].size
+    assert n > 140
+    rng = np.random.default_rng(12)
+    B = rng.normal(size=(70, n)) + 1j * rng.normal(size=(70, n))
+    x, rep = op.gmres(torch.from_numpy(B.reshape(-1)).cuda(), tol=1e-6, mode="block", block_steps=2)
+    assert rep.ok and np.all(rep.status == 0)
+    X = x.cpu().numpy().reshape(70, -1)
+    for r in (0, 33, 69):
+        assert np.linalg.norm(B[r] - A(X[r])) / np.linalg.norm(B[r]) <= 1e-6, r
+    op.close()
