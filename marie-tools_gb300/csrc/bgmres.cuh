@@ -256,7 +256,7 @@ struct BlockWork {
   int64_t part_cap = 0;
   float* tpart = nullptr;      // partial sums of the tensor-core path
   int64_t tpart_floats = 0;
-  bool tc = false;             // projections and Gram matrices on the tensor-core kernel
+  bool tc = false;             // projections on the tensor-core kernel (MARIE_BLOCK_PROJ=tcgen05)
 };
 
 // Offsets in the pinned buffer; the last 64 bytes hold the tensor-core
