@@ -140,7 +140,10 @@ def is_gmres_vie(A, b, restart, tol, maxit, x0, mode="fp64"):
     @(J) mvp_vie(J, EP, func, dims, fN), ie_solver_vie.m:15); ``b`` may hold
     several right-hand sides as columns (N_b x nrhs), solved in one batch.
     Returns x (like b), iter = [p, outit] per rhs and the relative residual
-    history (a list per rhs, or one array for a single rhs).
+    history (a list per rhs, or one array for a single rhs).  ``mode``:
+    "fp64" (the reference's arithmetic), "mixed" (complex64 GMRES per rhs
+    inside FP64 refinement) or "block" (the same refinement with one block
+    Krylov space for all columns of b; iter then counts block steps).
     """
     import torch
     if not isinstance(A, VieOperator):
