@@ -2,7 +2,7 @@
 the per-column residual norms of min_Y ||[S0; 0] - Hbar_j Y||_F after every
 block step j, the final Y and the residual block Z = [S0; 0] - Hbar Y, and
 the Cholesky factor / triangular inverse used by the block QR.  Compiled with
-the host compiler (no GPU)."""
+the host compiler (no GPU); p = 64 runs the reflector updates on host threads."""
 import os
 import shutil
 import subprocess
@@ -65,7 +65,7 @@ def _run(driver, tmp_path, p, m, S0, H, A):
     return res, Y, Z, ok, R, I
 
 
-@pytest.mark.parametrize("p,m", [(1, 6), (3, 5), (8, 4), (16, 3)])
+@pytest.mark.parametrize("p,m", [(1, 6), (3, 5), (8, 4), (16, 3), (64, 3)])
 def test_block_least_squares_matches_numpy(driver, tmp_path, p, m):
     S0, H, A = _case(p, m, seed=10 * p + m)
     res, Y, Z, ok, R, I = _run(driver, tmp_path, p, m, S0, H, A)
