@@ -3,8 +3,11 @@
 Workload (default): ellipsoid phantom on a 128^3 grid at 2 mm, PWL basis
 (12 unknowns/voxel), 297.2 MHz, 64 right-hand sides from 64 loop ports on a
 16 cm cylinder; Green's tensor with the accurate near zone (the reference's
-operator); complex64 GMRES(50) with FP32 accumulation inside an FP64
-iterative-refinement loop to 1e-6 relative residual.  One step = one batched
+operator); block GMRES over the 64 right-hand sides (one complex64 block
+Krylov space, 30 block steps per cycle, FP32 accumulation) inside an FP64
+iterative-refinement loop to 1e-6 relative residual (--solver mixed: one
+complex64 GMRES(50) per right-hand side instead; the line reports that
+solver on the same batch beside the block one).  One step = one batched
 solve of all right-hand sides, inputs resident in HBM.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -15,7 +18,8 @@ loop) and uneven16 (sixteen PWC phantoms with edges 48-128 and 1-8 loops
 each, the bodies on concurrent streams; reports the per-body residual
 spread).  --matvec-only times operator applications alone (the small,
 bounded command of the ncu captures), optionally from Tucker blocks
-(--tucker pre|apply).
+(--tucker pre|apply); --block-gemm M times the block solver's tensor-core
+projection kernel.
 
 Under torchrun each rank solves its own batch (replicas of the workload with
 rank-seeded loop jitter; no collective on the data path), value = solves of
