@@ -946,10 +946,11 @@ extern "C" marie_status marie_gmres_vie(marie_vie* h, const void* b_, void* x_, 
     const double floor_tol = o->inner_tol > 0 ? o->inner_tol : 1e-7;
     const int max_refine = o->max_refine > 0 ? o->max_refine : 10;
     // fraction of the outer target the inner solve aims for; a right-hand
-    // side that still misses tol gets another (short) inner solve.  At
-    // 128^3 PWL with 64 loop ports, tol 1e-6: 0.9 takes 238 batched
-    // per-RHS steps at 96^3 against 256 / 266 / 290 for 0.5 / 0.3 / 0.15,
-    // and 143 block steps at 128^3 against 154 / 175 for 0.5 / 0.2
+    // side that still misses tol gets another (short) inner solve.  With the
+    // 64 ring loop ports of the PWL phantom, tol 1e-6: per-RHS GMRES at 96^3
+    // takes 238 batched steps for 0.9 against 256 / 266 / 290 for 0.5 / 0.3
+    // / 0.15; block GMRES at 128^3 143 block steps against 154 / 175 for
+    // 0.5 / 0.2
     const double safety = o->inner_safety > 0 ? o->inner_safety : 0.9;
     for (int it = 0; it < max_refine; ++it) {
       std::vector<unsigned char> todo(nrhs, 0);
