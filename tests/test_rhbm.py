@@ -11,9 +11,13 @@ import pytest
 from oracle import marie_oracle as O
 from marie_gb300 import phantoms
 
-# read-only reference checkout (its data/bodies files); skipped where absent
-REF = Path(os.environ.get("MARIE_REFERENCE_ROOT", "/root/reference"))
-BODIES = REF / "data" / "bodies" / "Scatterers" / "2mm"
+# the reference checkout's body and input files, linked into oracle/_ref by
+# the oracle recipe (or MARIE_REFERENCE_ROOT); the tests that need them skip
+# without
+ROOT = Path(__file__).resolve().parent.parent
+_env = os.environ.get("MARIE_REFERENCE_ROOT")
+DATA = {k: (Path(_env) / "data" / k if _env else ROOT / "oracle" / "_ref" / k) for k in ("bodies", "inputs")}
+BODIES = DATA["bodies"] / "Scatterers" / "2mm"
 
 
 def _smooth31(v):
@@ -89,11 +93,11 @@ def test_load_inputs_synthetic(tmp_path):
     assert phantoms.larmor_frequency(3.0, "31p") == 17.235e6 * 3.0
 
 
-@pytest.mark.skipif(not (REF / "data" / "inputs").is_dir(), reason="reference input files not present")
+@pytest.mark.skipif(not DATA["inputs"].is_dir(), reason="reference input files not present")
 def test_reference_input_file():
     """The reference's own input file: 1H at 3.0063 T is 128 MHz (the first
     configuration's frequency), PWL basis, and its body file loads."""
-    inp = phantoms.load_inputs(REF / "data" / "inputs" / "inp_MSphere_HeadCoil1z.json")
+    inp = phantoms.load_inputs(DATA["inputs"] / "inp_MSphere_HeadCoil1z.json")
     assert abs(inp["freq"] - 128.0e6) < 0.1e6 and inp["pwl"] is True
     b = phantoms.load_rhbm(inp["body_file"])
     assert b.n == (121, 121, 121)
